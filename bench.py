@@ -1,0 +1,342 @@
+"""Benchmark of the Monte FDK hot path on GB300 (one JSON line on stdout).
+
+Workload (default): FDK at the recon-325 size -- 360 views of a 512 (u,
+in-plane) x 384 (v, axial) FP32 detector at 0.8 mm, SOD 500 mm, SDD 1000 mm,
+exact line integrals of 20 seeded random ellipsoids plus N(0, 0.01^2)
+noise, reconstructed into a 325^3 FP32 volume at 0.4 mm.  A step is one
+full FDK (weight + ramp filter + backprojection) of that stack.  The metric
+is GUPS: voxel-view updates (325^3 * 360) per second.
+
+  value  device-resident inputs, CUDA events around K steps on the context's
+         stream (inputs 283 MB > L2, so no extra L2 flush)
+  e2e    the same call through the C ABI with pinned host buffers: the
+         projection upload and the volume download are inside each step
+  --impl reference  the CPU oracle (a restatement of recon/bp3d20.cpp) on
+         all host cores over a bounded sample, scaled to GUPS
+
+Multi-GPU (torchrun): every rank reconstructs its own stack (replicas, weak
+scaling); the step time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--filter", default="auto", choices=["auto", "fp32", "bf16x3"])
+    ap.add_argument("--bp", default="tiled", choices=["plain", "tiled"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="reduced sizes (for profiling runs)")
+    return ap.parse_args()
+
+
+WORKLOAD = "fdk: 360 views x 512(u) x 384(v) FP32 @0.8mm, SOD 500, SDD 1000 mm -> 325^3 FP32 @0.4mm"
+
+
+def geometry(small=False):
+    from monte_gb300.abi import fdk_geom_recon325
+    if small:
+        return fdk_geom_recon325(n_views=90, nu=512, nv=384, n=163, voxel_mm=0.8)
+    return fdk_geom_recon325()
+
+
+def make_input(g, device):
+    from monte_gb300.phantoms import ellipsoid_line_integrals, random_ellipsoids
+    ell = random_ellipsoids(1002)
+    return ellipsoid_line_integrals(g, ell, noise_sigma=0.01, seed=1002, device=device)
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.dev)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+                power.append(float(p[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(g, budget_s=20.0):
+    """Time the CPU oracle (FP64 restatement of recon/bp3d20.cpp, all host
+    threads) on a bounded sample and scale to GUPS for the full workload:
+    the filter on a few views and the backprojection on a few z-slices of
+    all views; T = n_views * t_view + updates * t_update."""
+    import oracle
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    rng = np.random.Generator(np.random.PCG64(3))
+    nviews_s = 8
+    gs = g.copy()
+    gs.n_views = nviews_s
+    proj = rng.random((nviews_s, g.nu, g.nv), dtype=np.float32)
+    t0 = time.perf_counter()
+    oracle.fdk_filter(gs, proj)
+    t_view = (time.perf_counter() - t0) / nviews_s
+    filt = np.zeros((g.n_views, g.nv, g.nu), np.float32)
+    filt[:] = rng.random((g.nv, g.nu), dtype=np.float32)
+    nz_s = max(2, min(cores, 16))
+    t0 = time.perf_counter()
+    oracle.fdk_backproject(g, filt, z_range=(g.nz // 2, g.nz // 2 + nz_s))
+    t_bp = time.perf_counter() - t0
+    upd_s = nz_s * g.nx * g.ny * g.n_views
+    t_upd = t_bp / upd_s
+    updates = g.nx * g.ny * g.nz * g.n_views
+    T = g.n_views * t_view + updates * t_upd
+    return {"value": updates / T / 1e9, "unit": "GUPS", "cores": cores, "kind": "port",
+            "sample": "oracle filter on %d views + backprojection of %d z-slices x %d views, "
+                      "scaled to the full workload (est. %.1f s per FDK)" % (nviews_s, nz_s,
+                                                                            g.n_views, T)}
+
+
+def run_reference(args):
+    world, rank, local = dist_setup(args)
+    if rank != 0:
+        return
+    g = geometry(args.small)
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(g)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": "FDK GUPS (voxel-view updates/s)", "value": v,
+            "unit": "GUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "GUPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from monte_gb300 import abi
+    from monte_gb300.lib import Context
+    g = geometry(args.small)
+    stream = torch.cuda.current_stream(dev)
+    ctx = Context(local, stream=stream)
+    fmode = {"auto": abi.MONTE_FILTER_BF16X3, "fp32": abi.MONTE_FILTER_FP32,
+             "bf16x3": abi.MONTE_FILTER_BF16X3}[args.filter]
+    if args.filter == "auto":
+        try:  # the tensor-core filter needs nu % 64 == 0 and nv % 128 == 0
+            pt = torch.zeros((1, 64, 128), device=dev)
+            gt = g.copy()
+            gt.n_views, gt.nu, gt.nv = 1, 64, 128
+            ctx.fdk_filter(gt, pt, torch.empty_like(pt), mode=fmode)
+        except Exception:
+            fmode = abi.MONTE_FILTER_FP32
+    bmode = abi.MONTE_BP_TILED if args.bp == "tiled" else abi.MONTE_BP_PLAIN
+
+    proj = make_input(g, dev)
+    filt = torch.empty((g.n_views, g.nv, g.nu), dtype=torch.float32, device=dev)
+    vol = torch.empty((g.nz, g.ny, g.nx), dtype=torch.float32, device=dev)
+    updates = g.nx * g.ny * g.nz * g.n_views
+
+    def step():
+        ctx.fdk_filter(g, proj, filt, mode=fmode)
+        ctx.fdk_backproject(g, filt, vol, mode=bmode)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    clocks = Clocks(local)
+    clocks.start()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t_all0 = torch.cuda.Event(enable_timing=True)
+    t_all1 = torch.cuda.Event(enable_timing=True)
+    t_all0.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        ctx.fdk_filter(g, proj, filt, mode=fmode)
+        ev[i][1].record(stream)
+        ctx.fdk_backproject(g, filt, vol, mode=bmode)
+        ev[i][2].record(stream)
+    t_all1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop()
+    elapsed = t_all0.elapsed_time(t_all1) / 1e3
+    elapsed = max_over_ranks(elapsed, world, dev)
+    t_filter = statistics.mean(e[0].elapsed_time(e[1]) for e in ev) / 1e3
+    t_bp = statistics.mean(e[1].elapsed_time(e[2]) for e in ev) / 1e3
+    ms_per_step = elapsed / args.steps * 1e3
+    value = world * updates * args.steps / elapsed / 1e9
+
+    # end to end through the C ABI with pinned host buffers
+    h_proj = proj.cpu().pin_memory()
+    h_vol = torch.empty((g.nz, g.ny, g.nx), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        ctx.fdk(g, h_proj, h_vol, filter_mode=fmode, bp_mode=bmode)
+    barrier(world)
+    t0 = time.perf_counter()
+    n_e2e = max(3, args.steps // 2)
+    for _ in range(n_e2e):
+        ctx.fdk(g, h_proj, h_vol, filter_mode=fmode, bp_mode=bmode)
+    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(t_e2e, world, dev)
+    e2e_val = world * updates * n_e2e / t_e2e / 1e9
+    del h_vol
+
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s
+    bp_flops = 10.0 * updates
+    bp_bytes = g.n_views * g.nu * g.nv * 4 + g.nx * g.ny * g.nz * 4
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    prof = {}
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            prof = json.load(f)
+    except OSError:
+        pass
+    traffic = prof.get("bp_tiled" if bmode == abi.MONTE_BP_TILED else "bp_plain")
+
+    line = {
+        "metric": "FDK GUPS (voxel-view updates/s)", "value": value, "unit": "GUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD if not args.small else "reduced (profiling) " + WORKLOAD,
+                   "filter": {abi.MONTE_FILTER_FP32: "fp32", abi.MONTE_FILTER_BF16X3: "bf16x3"}[fmode],
+                   "backprojector": args.bp, "l2": "inputs 283 MB > 129 MB L2 (no flush)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "breakdown_ms": {"filter": t_filter * 1e3, "backprojection": t_bp * 1e3},
+        "roofline": {"kernel": "backprojection", "bound": "fp32",
+                     "achieved": bp_flops / t_bp / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": bp_flops / t_bp / 1e12 / fp32_peak, "traffic": traffic,
+                     "peak_source": "%d SMs x 128 FP32 lanes x 2 x %.0f MHz (sm_max_mhz of "
+                                    "MEASURED_PEAKS.json)" % (n_sm, sm_max),
+                     "algorithmic": "10 flop per voxel-view update"},
+        "roofline_hbm": {"kernel": "backprojection", "bound": "hbm",
+                         "achieved": bp_bytes / t_bp / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": bp_bytes / t_bp / 1e9 / hbm_peak, "traffic": traffic},
+        "e2e": {"value": e2e_val, "unit": "GUPS",
+                "h2d_bytes_per_step": int(g.n_views * g.nu * g.nv * 4),
+                "d2h_bytes_per_step": int(g.nx * g.ny * g.nz * 4)},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(g)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,329 @@
+// fdk_api.cu -- C-ABI entry points of the FDK path (include/monte.h):
+// argument checks, per-geometry device tables, host staging, launches.
+//
+// Reference programs: recon/bp3d20.cpp (65x65 detector) and
+// recon/bp3d20_325.cpp (325x325), whose main() reads the projection file,
+// weights, filters, backprojects and writes three raw files
+// (recon/bp3d20.cpp:15-194).  Here the same three stages run on the GPU
+// behind monte_fdk_filter / monte_fdk_backproject / monte_fdk.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fdk.cuh"
+#include "monte_internal.h"
+
+namespace monte {
+
+FdkDev make_fdk_dev(const monte_fdk_geom& g) {
+  FdkDev d;
+  d.n_views = g.n_views;
+  d.nu = g.nu;
+  d.nv = g.nv;
+  d.nx = g.nx;
+  d.ny = g.ny;
+  d.nz = g.nz;
+  d.s_begin = g.s_begin;
+  d.s_end = g.s_end;
+  d.mask_r2 = g.mask_radius > 0 ? g.mask_radius * g.mask_radius : 0;
+  d.cs = g.nx / 2;
+  d.ct = g.ny / 2;
+  d.cz = g.nz / 2;
+  d.flags = g.flags;
+  d.x0 = (float)g.x0;
+  d.y0 = (float)g.y0;
+  d.z0 = (float)g.z0;
+  d.dvox = (float)g.dvox;
+  d.sdd = (float)g.sdd;
+  d.D = (float)g.wdist;
+  d.half_u = (float)g.half_u;
+  d.half_v = (float)g.half_v;
+  d.inv_du = (float)(1.0 / g.du);
+  d.inv_dv = (float)(1.0 / g.dv);
+  // recon/bp3d20.cpp:116 rejects |u'|>half_u, |v'|>half_v; :152 then needs
+  // 0 <= x <= nv and 0 <= y <= nu.
+  d.xmax = (float)std::fmin((double)g.nv, 2.0 * g.half_v / g.dv);
+  d.ymax = (float)std::fmin((double)g.nu, 2.0 * g.half_u / g.du);
+  return d;
+}
+
+namespace {
+
+int validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid) {
+  if (!g) return set_error(ctx, MONTE_EINVAL, "geometry is NULL");
+  if (g->n_views <= 0 || g->nu <= 0 || g->nv <= 0)
+    return set_error(ctx, MONTE_EINVAL, "bad detector size views=%d nu=%d nv=%d", g->n_views,
+                     g->nu, g->nv);
+  if (!(g->du > 0) || !(g->dv > 0) || !(g->sdd > 0) || !(g->sod > 0) || !(g->half_u > 0) ||
+      !(g->half_v > 0))
+    return set_error(ctx, MONTE_EINVAL, "non-positive detector pitch/extent or distance");
+  if (g->flags & ~(MONTE_FDK_TAN_DEGREES | MONTE_FDK_FLAT_EDGE))
+    return set_error(ctx, MONTE_EINVAL, "unknown FDK flags 0x%x", g->flags);
+  size_t n;
+  if (!mul_ok((size_t)g->n_views, (size_t)g->nu, &n) || !mul_ok(n, (size_t)g->nv, &n) ||
+      n > ((size_t)1 << 40))
+    return set_error(ctx, MONTE_EOVERFLOW, "projection stack too large");
+  if ((size_t)g->nu * g->nv > (size_t)INT32_MAX)
+    return set_error(ctx, MONTE_EOVERFLOW, "detector too large");
+  if (need_grid) {
+    if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0)
+      return set_error(ctx, MONTE_EINVAL, "bad grid %d x %d x %d", g->nx, g->ny, g->nz);
+    if (g->s_begin < 0 || g->s_end > g->nx || g->s_begin > g->s_end)
+      return set_error(ctx, MONTE_EINVAL, "bad slab [%d,%d) for nx=%d", g->s_begin, g->s_end,
+                       g->nx);
+    if (!(g->dvox > 0)) return set_error(ctx, MONTE_EINVAL, "non-positive voxel pitch");
+    if (!mul_ok((size_t)g->nx, (size_t)g->ny, &n) || !mul_ok(n, (size_t)g->nz, &n) ||
+        n > ((size_t)1 << 40))
+      return set_error(ctx, MONTE_EOVERFLOW, "volume too large");
+  }
+  return MONTE_OK;
+}
+
+// Upload per-view constants, weight table and taps for geometry g (cached).
+int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
+  std::vector<uint8_t> key(sizeof(monte_fdk_geom));
+  memcpy(key.data(), g, sizeof(monte_fdk_geom));
+  if (key == ctx->fdk_key && ctx->fdk_views.ptr) return MONTE_OK;
+  const int nv_ = g->n_views, nu = g->nu, nv = g->nv;
+  std::vector<BpView> views(nv_);
+  float beta_span = (float)(360.0 / nv_);
+  for (int k = 0; k < nv_; k++) {
+    double beta = (double)k * 360.0 / nv_;
+    double a = M_PI * beta / 180;
+    double c = cos(a), s = sin(a);
+    float start_x = (float)(-g->sod);
+    double tanb = (g->flags & MONTE_FDK_TAN_DEGREES) ? tan(beta) : tan(a);
+    BpView& v = views[k];
+    v.c = (float)c;
+    v.s = (float)s;
+    v.px = (float)(start_x * c);
+    v.py = (float)(start_x * s);
+    v.tanb = (float)tanb;
+    v.rs = (float)(1.0 / sqrt(1 + tanb * tanb));
+    v.factor = (float)(beta_span * 2 * M_PI / 360 * g->scale * g->scale2);
+    v.pad = 0.f;
+  }
+  // cosine weights w[u][v] (recon/bp3d20.cpp:40)
+  std::vector<float> w((size_t)nu * nv);
+  for (int a = 0; a < nu; a++)
+    for (int b = 0; b < nv; b++) {
+      double D = g->wdist;
+      double pu = -1 * (a * g->du) + g->half_u;
+      double pv = (b * g->dv) - g->half_v;
+      w[(size_t)a * nv + b] = (float)(D / sqrt(D * D + pu * pu + pv * pv));
+    }
+  // taps 0.5*h[n] at index nu-1+n (recon/bp3d20.cpp:48-60,68)
+  std::vector<float> taps(2 * nu - 1);
+  taps[nu - 1] = 0.125f;
+  for (int n = 1; n < nu; n++) {
+    float h = 0.f;
+    if (n % 2 == 1) {
+      double x = n * M_PI;
+      h = (float)(-1. / (x * x));
+    }
+    taps[nu - 1 + n] = taps[nu - 1 - n] = 0.5f * h;
+  }
+  MONTE_TRY(ensure(ctx, ctx->fdk_views, views.size() * sizeof(BpView), "view table"));
+  MONTE_TRY(ensure(ctx, ctx->fdk_weights, w.size() * sizeof(float), "weight table"));
+  MONTE_TRY(ensure(ctx, ctx->fdk_taps, taps.size() * sizeof(float), "tap table"));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_views.ptr, views.data(), views.size() * sizeof(BpView),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_weights.ptr, w.data(), w.size() * sizeof(float),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_taps.ptr, taps.data(), taps.size() * sizeof(float),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  if (bf16x3_supported(make_fdk_dev(*g))) {
+    std::vector<uint16_t> bs(bf16x3_bsplit_bytes(nu) / 2);
+    bf16x3_build_bsplit(nu, taps.data(), bs.data());
+    MONTE_TRY(ensure(ctx, ctx->fdk_bsplit, bs.size() * 2, "split Toeplitz operand"));
+    MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_bsplit.ptr, bs.data(), bs.size() * 2,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+  }
+  // the host vectors die at return: make the copies complete first
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->fdk_key = key;
+  return MONTE_OK;
+}
+
+int run_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_proj, float* d_filtered,
+               int filter_mode) {
+  FdkDev d = make_fdk_dev(*g);
+  cudaError_t e;
+  if (filter_mode == MONTE_FILTER_FP32) {
+    e = launch_fdk_filter_fp32(d, d_proj, (const float*)ctx->fdk_weights.ptr,
+                               (const float*)ctx->fdk_taps.ptr, d_filtered, ctx->stream);
+  } else if (filter_mode == MONTE_FILTER_BF16X3) {
+    if (!bf16x3_supported(d))
+      return set_error(ctx, MONTE_EUNSUPPORTED,
+                       "BF16x3 filter needs nu %% 64 == 0 and nv %% 128 == 0 (got %d, %d)", g->nu,
+                       g->nv);
+    e = launch_fdk_filter_bf16x3(d, d_proj, (const float*)ctx->fdk_weights.ptr,
+                                 (const uint16_t*)ctx->fdk_bsplit.ptr, d_filtered, ctx->d_status,
+                                 ctx->sm_count, ctx->stream);
+  } else {
+    return set_error(ctx, MONTE_EINVAL, "unknown filter mode %d", filter_mode);
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "filter launch");
+  return MONTE_OK;
+}
+
+int run_bp(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_filtered, float* d_xy,
+           float* d_zy, int bp_mode) {
+  FdkDev d = make_fdk_dev(*g);
+  const size_t vol = (size_t)g->nx * g->ny * g->nz * sizeof(float);
+  if (g->s_begin != 0 || g->s_end != g->nx) {
+    MONTE_CUDA(ctx, cudaMemsetAsync(d_xy, 0, vol, ctx->stream));
+    if (d_zy) MONTE_CUDA(ctx, cudaMemsetAsync(d_zy, 0, vol, ctx->stream));
+  }
+  cudaError_t e;
+  const BpView* views = (const BpView*)ctx->fdk_views.ptr;
+  if (bp_mode == MONTE_BP_PLAIN) {
+    e = launch_fdk_bp_plain(d, views, d_filtered, d_xy, d_zy, ctx->stream);
+  } else if (bp_mode == MONTE_BP_TILED) {
+    int variant = ctx->bp_tune_choice;
+    if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
+    if (!fdk_bp_tiled_supported(d, variant)) {
+      e = launch_fdk_bp_plain(d, views, d_filtered, d_xy, d_zy, ctx->stream);
+    } else {
+      e = launch_fdk_bp_tiled(d, views, d_filtered, d_xy, d_zy, variant, ctx->stream);
+    }
+  } else {
+    return set_error(ctx, MONTE_EINVAL, "unknown backprojection mode %d", bp_mode);
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "backprojection launch");
+  return MONTE_OK;
+}
+
+size_t proj_bytes(const monte_fdk_geom* g) {
+  return (size_t)g->n_views * g->nu * g->nv * sizeof(float);
+}
+size_t vol_bytes(const monte_fdk_geom* g) {
+  return (size_t)g->nx * g->ny * g->nz * sizeof(float);
+}
+
+}  // namespace
+}  // namespace monte
+
+using namespace monte;
+
+extern "C" {
+
+void monte_fdk_geom_reference65(monte_fdk_geom* g) {
+  if (!g) return;
+  memset(g, 0, sizeof(*g));
+  g->n_views = 360;  // recon/bp3d20.cpp:19
+  g->nu = g->nv = 65;  // :17
+  g->flags = MONTE_FDK_TAN_DEGREES | MONTE_FDK_FLAT_EDGE;
+  g->du = g->dv = 0.5;  // :40,123-124
+  g->half_u = g->half_v = 16.25;
+  g->sod = 160;  // :85
+  g->sdd = 220;  // :107
+  g->wdist = 60;  // :40,159
+  g->nx = g->ny = g->nz = 256;  // :18
+  g->s_begin = 125;  // :93
+  g->s_end = 130;
+  g->dvox = 0.1;  // :96-98
+  g->x0 = -12.8;
+  g->y0 = 12.8;
+  g->z0 = 12.8;
+  g->mask_radius = 118;  // :145
+  g->scale = 2.7;  // :160
+  g->scale2 = 1.0;
+}
+
+void monte_fdk_geom_reference325(monte_fdk_geom* g) {
+  if (!g) return;
+  monte_fdk_geom_reference65(g);
+  g->nu = g->nv = 325;  // recon/bp3d20_325.cpp:17
+  g->du = g->dv = 0.1;  // :43,134-135
+  g->mask_radius = 0;   // the sphere test of bp3d20.cpp:145 is dropped
+  g->scale = 2.7;       // :170
+  g->scale2 = 5.0;
+}
+
+int monte_fdk_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
+                     int filter_mode, int mem) {
+  if (!ctx) return MONTE_EINVAL;
+  MONTE_TRY(validate(ctx, g, false));
+  if (!proj || !filtered) return set_error(ctx, MONTE_EINVAL, "null projection/filtered pointer");
+  if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
+    return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(prepare_tables(ctx, g));
+  if (mem == MONTE_MEM_DEVICE) return run_filter(ctx, g, proj, filtered, filter_mode);
+  const size_t pb = proj_bytes(g);
+  MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
+  MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
+  float* dp = (float*)ctx->scratch[kScratchProj].ptr;
+  float* df = (float*)ctx->scratch[kScratchFiltered].ptr;
+  MONTE_CUDA(ctx, cudaMemcpyAsync(dp, proj, pb, cudaMemcpyHostToDevice, ctx->stream));
+  MONTE_TRY(run_filter(ctx, g, dp, df, filter_mode));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(filtered, df, pb, cudaMemcpyDeviceToHost, ctx->stream));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MONTE_OK;
+}
+
+int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* filtered,
+                          float* vol_xy, float* vol_zy, int bp_mode, int mem) {
+  if (!ctx) return MONTE_EINVAL;
+  MONTE_TRY(validate(ctx, g, true));
+  if (!filtered || !vol_xy) return set_error(ctx, MONTE_EINVAL, "null filtered/volume pointer");
+  if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
+    return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(prepare_tables(ctx, g));
+  if (mem == MONTE_MEM_DEVICE) return run_bp(ctx, g, filtered, vol_xy, vol_zy, bp_mode);
+  const size_t pb = proj_bytes(g), vb = vol_bytes(g);
+  MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
+  MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "volume staging"));
+  if (vol_zy) MONTE_TRY(ensure_slot(ctx, kScratchVolZY, vb, "volume staging"));
+  float* df = (float*)ctx->scratch[kScratchFiltered].ptr;
+  float* dxy = (float*)ctx->scratch[kScratchVolXY].ptr;
+  float* dzy = vol_zy ? (float*)ctx->scratch[kScratchVolZY].ptr : nullptr;
+  MONTE_CUDA(ctx, cudaMemcpyAsync(df, filtered, pb, cudaMemcpyHostToDevice, ctx->stream));
+  MONTE_TRY(run_bp(ctx, g, df, dxy, dzy, bp_mode));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(vol_xy, dxy, vb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (vol_zy) MONTE_CUDA(ctx, cudaMemcpyAsync(vol_zy, dzy, vb, cudaMemcpyDeviceToHost, ctx->stream));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MONTE_OK;
+}
+
+int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
+              float* vol_xy, float* vol_zy, int filter_mode, int bp_mode, int mem) {
+  if (!ctx) return MONTE_EINVAL;
+  MONTE_TRY(validate(ctx, g, true));
+  if (!proj || !vol_xy) return set_error(ctx, MONTE_EINVAL, "null projection/volume pointer");
+  if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
+    return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(prepare_tables(ctx, g));
+  const size_t pb = proj_bytes(g), vb = vol_bytes(g);
+  if (mem == MONTE_MEM_DEVICE) {
+    float* df = filtered;
+    if (!df) {
+      MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered scratch"));
+      df = (float*)ctx->scratch[kScratchFiltered].ptr;
+    }
+    MONTE_TRY(run_filter(ctx, g, proj, df, filter_mode));
+    return run_bp(ctx, g, df, vol_xy, vol_zy, bp_mode);
+  }
+  MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
+  MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
+  MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "volume staging"));
+  if (vol_zy) MONTE_TRY(ensure_slot(ctx, kScratchVolZY, vb, "volume staging"));
+  float* dp = (float*)ctx->scratch[kScratchProj].ptr;
+  float* df = (float*)ctx->scratch[kScratchFiltered].ptr;
+  float* dxy = (float*)ctx->scratch[kScratchVolXY].ptr;
+  float* dzy = vol_zy ? (float*)ctx->scratch[kScratchVolZY].ptr : nullptr;
+  MONTE_CUDA(ctx, cudaMemcpyAsync(dp, proj, pb, cudaMemcpyHostToDevice, ctx->stream));
+  MONTE_TRY(run_filter(ctx, g, dp, df, filter_mode));
+  MONTE_TRY(run_bp(ctx, g, df, dxy, dzy, bp_mode));
+  if (filtered)
+    MONTE_CUDA(ctx, cudaMemcpyAsync(filtered, df, pb, cudaMemcpyDeviceToHost, ctx->stream));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(vol_xy, dxy, vb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (vol_zy) MONTE_CUDA(ctx, cudaMemcpyAsync(vol_zy, dzy, vb, cudaMemcpyDeviceToHost, ctx->stream));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MONTE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+"""Python front end of libmonte.so (ctypes over the C ABI in include/monte.h).
+
+Arrays are passed as torch CUDA tensors (device memory, MONTE_MEM_DEVICE)
+or as numpy arrays / CPU tensors (host memory, MONTE_MEM_HOST).  There is
+no fallback: if libmonte.so is missing or no GPU is usable, calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import FdkGeom
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmonte.so")
+_LIB = None
+
+
+class MonteError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("monte error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(build_if_missing=False):
+    """Load libmonte.so (raises if it is missing and build_if_missing is
+    False)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise MonteError(abi.MONTE_EUNSUPPORTED,
+                             "libmonte.so not built (run monte_gb300.build.build())")
+        from .build import build
+        build()
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    G = C.POINTER(FdkGeom)
+    lib.monte_abi_version.restype = C.c_int
+    lib.monte_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    lib.monte_ctx_destroy.argtypes = [P]
+    lib.monte_last_error.argtypes = [P]
+    lib.monte_last_error.restype = C.c_char_p
+    lib.monte_ctx_set_stream.argtypes = [P, P]
+    lib.monte_ctx_synchronize.argtypes = [P]
+    lib.monte_fdk_geom_reference65.argtypes = [G]
+    lib.monte_fdk_geom_reference65.restype = None
+    lib.monte_fdk_geom_reference325.argtypes = [G]
+    lib.monte_fdk_geom_reference325.restype = None
+    lib.monte_fdk_filter.argtypes = [P, G, P, P, C.c_int, C.c_int]
+    lib.monte_fdk_backproject.argtypes = [P, G, P, P, P, C.c_int, C.c_int]
+    lib.monte_fdk.argtypes = [P, G, P, P, P, P, C.c_int, C.c_int, C.c_int]
+    _LIB = lib
+    return lib
+
+
+def _ptr(a):
+    """(address, mem) of a torch tensor or numpy array; None -> (None, None)."""
+    if a is None:
+        return None, None
+    if isinstance(a, np.ndarray):
+        assert a.flags.c_contiguous
+        return a.ctypes.data, abi.MONTE_MEM_HOST
+    # torch tensor
+    assert a.is_contiguous()
+    return a.data_ptr(), (abi.MONTE_MEM_DEVICE if a.is_cuda else abi.MONTE_MEM_HOST)
+
+
+def _mem_of(*arrays):
+    mems = {m for _, m in (_ptr(a) for a in arrays if a is not None)}
+    if len(mems) != 1:
+        raise ValueError("all arrays of one call must live in the same memory space")
+    return mems.pop()
+
+
+class Context:
+    """One libmonte context (device + stream).  Use torch's current stream
+    for device work by passing stream=torch.cuda.current_stream()."""
+
+    def __init__(self, device=0, stream=None):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.monte_ctx_create(C.byref(h), device)
+        if rc != 0:
+            raise MonteError(rc, self.lib.monte_last_error(None).decode())
+        self.h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.monte_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, rc):
+        if rc != 0:
+            raise MonteError(rc, self.lib.monte_last_error(self.h).decode())
+        return rc
+
+    def set_stream(self, stream):
+        handle = getattr(stream, "cuda_stream", stream)
+        self.check(self.lib.monte_ctx_set_stream(self.h, C.c_void_p(handle)))
+
+    def synchronize(self):
+        self.check(self.lib.monte_ctx_synchronize(self.h))
+
+    # ---- FDK ----------------------------------------------------------
+    def fdk_filter(self, g, proj, filtered, mode=abi.MONTE_FILTER_FP32):
+        mem = _mem_of(proj, filtered)
+        self.check(self.lib.monte_fdk_filter(self.h, C.byref(g), _ptr(proj)[0],
+                                             _ptr(filtered)[0], mode, mem))
+
+    def fdk_backproject(self, g, filtered, vol_xy, vol_zy=None, mode=abi.MONTE_BP_PLAIN):
+        mem = _mem_of(filtered, vol_xy, vol_zy)
+        self.check(self.lib.monte_fdk_backproject(self.h, C.byref(g), _ptr(filtered)[0],
+                                                  _ptr(vol_xy)[0], _ptr(vol_zy)[0], mode, mem))
+
+    def fdk(self, g, proj, vol_xy, filtered=None, vol_zy=None,
+            filter_mode=abi.MONTE_FILTER_FP32, bp_mode=abi.MONTE_BP_PLAIN):
+        mem = _mem_of(proj, vol_xy, filtered, vol_zy)
+        self.check(self.lib.monte_fdk(self.h, C.byref(g), _ptr(proj)[0], _ptr(filtered)[0],
+                                      _ptr(vol_xy)[0], _ptr(vol_zy)[0], filter_mode, bp_mode,
+                                      mem))

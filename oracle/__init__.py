@@ -1,0 +1,88 @@
+"""CPU oracle for the Monte hot paths -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package, and only to check or to time the reference algorithm on the
+host; the product (monte_gb300, libmonte.so) never calls it.
+
+liboracle.so is built from the C restatements in this directory
+(fdk_oracle.c, ...) by oracle/Makefile.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from monte_gb300.abi import FdkGeom
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        _LIB = C.CDLL(path)
+        f = C.POINTER(C.c_float)
+        d = C.POINTER(C.c_double)
+        g = C.POINTER(FdkGeom)
+        _LIB.oracle_fdk_taps.argtypes = [C.c_int, f]
+        _LIB.oracle_fdk_filter.argtypes = [g, f, f]
+        _LIB.oracle_fdk_filter_f64.argtypes = [g, f, d]
+        _LIB.oracle_fdk_backproject.argtypes = [g, f, f, f, C.c_int, C.c_int]
+        _LIB.oracle_fdk_backproject_f64.argtypes = [g, d, d, C.c_int, C.c_int]
+    return _LIB
+
+
+def _fp(a):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def fdk_taps(nu):
+    out = np.zeros(2 * nu - 1, np.float32)
+    lib().oracle_fdk_taps(nu, _fp(out))
+    return out
+
+
+def fdk_filter(g, proj, precise=False):
+    """proj[view][u][v] float32 -> filtered[view][v][u] (float32, or float64
+    when precise)."""
+    proj = np.ascontiguousarray(proj, np.float32)
+    assert proj.shape == (g.n_views, g.nu, g.nv)
+    if precise:
+        out = np.zeros((g.n_views, g.nv, g.nu), np.float64)
+        lib().oracle_fdk_filter_f64(C.byref(g), _fp(proj), _dp(out))
+    else:
+        out = np.zeros((g.n_views, g.nv, g.nu), np.float32)
+        lib().oracle_fdk_filter(C.byref(g), _fp(proj), _fp(out))
+    return out
+
+
+def fdk_backproject(g, filtered, z_range=None, zy=False):
+    """filtered[view][v][u] -> vol_xy[nz][ny][nx] (and vol_zy[nx][ny][nz]).
+    float32 input: the reference's own arithmetic; float64 input: FP64."""
+    z0, z1 = z_range if z_range is not None else (0, g.nz)
+    if filtered.dtype == np.float64:
+        filtered = np.ascontiguousarray(filtered)
+        vol = np.zeros((g.nz, g.ny, g.nx), np.float64)
+        lib().oracle_fdk_backproject_f64(C.byref(g), _dp(filtered), _dp(vol), z0, z1)
+        return vol
+    filtered = np.ascontiguousarray(filtered, np.float32)
+    vol = np.zeros((g.nz, g.ny, g.nx), np.float32)
+    vzy = np.zeros((g.nx, g.ny, g.nz), np.float32) if zy else None
+    lib().oracle_fdk_backproject(C.byref(g), _fp(filtered), _fp(vol),
+                                 _fp(vzy) if zy else None, z0, z1)
+    return (vol, vzy) if zy else vol

@@ -1,0 +1,101 @@
+"""FDK on the GPU through the C ABI against the reference programs' output
+(golden fixtures) and the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from helpers import golden, past_end_voxels, rel_rms
+from inputs import fdk_projections
+from monte_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+FILTERS = [abi.MONTE_FILTER_FP32]
+BPS = [abi.MONTE_BP_PLAIN, abi.MONTE_BP_TILED]
+
+
+def _run(ctx, g, proj, filter_mode=abi.MONTE_FILTER_FP32, bp_mode=abi.MONTE_BP_PLAIN, zy=False):
+    p = torch.from_numpy(proj).cuda()
+    f = torch.empty((g.n_views, g.nv, g.nu), dtype=torch.float32, device="cuda")
+    xy = torch.empty((g.nz, g.ny, g.nx), dtype=torch.float32, device="cuda")
+    vzy = torch.empty((g.nx, g.ny, g.nz), dtype=torch.float32, device="cuda") if zy else None
+    ctx.fdk(g, p, xy, filtered=f, vol_zy=vzy, filter_mode=filter_mode, bp_mode=bp_mode)
+    ctx.synchronize()
+    out = [f.cpu().numpy(), xy.cpu().numpy()]
+    if zy:
+        out.append(vzy.cpu().numpy())
+    return out
+
+
+@pytest.mark.parametrize("bp_mode", BPS)
+def test_fdk65_matches_reference_program(ctx, bp_mode):
+    g = abi.fdk_geom_reference65()
+    gold = golden("fdk65")
+    proj = fdk_projections(360, 65, 65, int(gold["seed"]))
+    f, xy, zy = _run(ctx, g, proj, bp_mode=bp_mode, zy=True)
+    assert rel_rms(f[gold["view_ids"]], gold["filtered_views"]) < 1e-6
+    keep = ~past_end_voxels(g)[:, :, 125:130]
+    slab = xy[:, :, 125:130]
+    assert rel_rms(slab[keep], gold["xy_slab"][keep]) < 1e-5
+    assert not np.any(xy[:, :, :125]) and not np.any(xy[:, :, 130:])
+    assert np.array_equal(zy, xy.transpose(2, 1, 0))
+
+
+@pytest.mark.parametrize("bp_mode", BPS)
+def test_fdk325_matches_reference_program(ctx, bp_mode):
+    g = abi.fdk_geom_reference325()
+    gold = golden("fdk325")
+    proj = fdk_projections(360, 325, 325, int(gold["seed"]))
+    f, xy = _run(ctx, g, proj, bp_mode=bp_mode)
+    got = f[gold["view_ids"]][:, gold["row_ids"], :]
+    assert rel_rms(got, gold["filtered_rows"]) < 1e-6
+    keep = ~past_end_voxels(g)[:, :, 125:130]
+    assert rel_rms(xy[:, :, 125:130][keep], gold["xy_slab"][keep]) < 1e-5
+
+
+def _small_recon_geom():
+    # the recon-325 conventions at a size the FP64 oracle finishes quickly
+    return abi.fdk_geom_recon325(n_views=360, nu=128, nv=96, pitch_mm=3.2, n=81,
+                                 voxel_mm=1.6)
+
+
+@pytest.mark.parametrize("bp_mode", BPS)
+def test_full_volume_against_fp64_oracle(ctx, bp_mode):
+    g = _small_recon_geom()
+    proj = fdk_projections(g.n_views, g.nu, g.nv, 2024)
+    f, xy = _run(ctx, g, proj, bp_mode=bp_mode)
+    f64 = oracle.fdk_filter(g, proj, precise=True)
+    assert rel_rms(f, f64) < 1e-6
+    v64 = oracle.fdk_backproject(g, f64)
+    err = rel_rms(xy, v64)
+    assert err < 1e-5, err
+
+
+def test_host_memory_path_equals_device_path(ctx):
+    g = abi.fdk_geom_reference65()
+    proj = fdk_projections(360, 65, 65, 11)
+    f_d, xy_d = _run(ctx, g, proj)
+    f_h = np.zeros((g.n_views, g.nv, g.nu), np.float32)
+    xy_h = np.zeros((g.nz, g.ny, g.nx), np.float32)
+    ctx.fdk(g, proj, xy_h, filtered=f_h)
+    assert np.array_equal(f_h, f_d) and np.array_equal(xy_h, xy_d)
+
+
+def test_bad_arguments_are_rejected(ctx):
+    from monte_gb300.lib import MonteError
+    g = abi.fdk_geom_reference65()
+    g.nu = 0
+    p = torch.zeros(10, device="cuda")
+    with pytest.raises(MonteError) as e:
+        ctx.fdk(g, p, p, filtered=p)
+    assert e.value.code == abi.MONTE_EINVAL
+    g = abi.fdk_geom_reference65()
+    g.s_end = 300
+    with pytest.raises(MonteError) as e:
+        ctx.fdk(g, p, p, filtered=p)
+    assert e.value.code == abi.MONTE_EINVAL
+    g = abi.fdk_geom_reference65()
+    with pytest.raises(MonteError) as e:
+        ctx.fdk(g, p, p, filtered=p, filter_mode=7)
+    assert e.value.code == abi.MONTE_EINVAL
