@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--filter", default="auto", choices=["auto", "fp32", "bf16x3"])
     ap.add_argument("--bp", default="tiled", choices=["plain", "tiled"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form FDK timing")
+    ap.add_argument("--no-mc", action="store_true", help="skip the Monte Carlo timing")
     ap.add_argument("--small", action="store_true", help="reduced sizes (for profiling runs)")
     return ap.parse_args()
 
@@ -178,6 +180,55 @@ def cpu_baseline(g, budget_s=20.0):
                                                                             g.n_views, T)}
 
 
+MC_WORKLOAD = ("mc: 325^3 labels @0.8mm (water / Ca-water bone 1.5-1.9 / air, 20 seeded "
+               "ellipsoids), 20-80 keV lines weighted (80-E), 512x384 pixels @0.8mm, SOD 500, "
+               "SDD 1000 mm, 509 histories per pixel per view (1.0e8 per view), 5 interactions")
+
+
+def mc_inputs(device):
+    import torch
+    from monte_gb300 import abi, phantoms
+    x = np.load(os.path.join(REPO, "tests", "golden", "xcom.npz"))
+    lab, vox, org, dens, mats = phantoms.ellipsoid_labels()
+    E = np.arange(20.0, 81.0)
+    inp = abi.McInputs(torch.from_numpy(lab).to(device), vox, org, mats, dens,
+                       [x["water"], x["ca"]], E, 80.0 - E)
+    g = abi.mc_geom(360, 512, 384, 0.08, 50.0, 100.0, 14.0, flags=abi.MONTE_MC_STALE_SIN_PHI)
+    return g, inp
+
+
+def mc_bench(ctx, device, steps=3, per=509):
+    """Histories/s of the persistent and the plain Monte Carlo kernels on one
+    view of the 325^3 workload (1.0e8 histories per step)."""
+    import torch
+    from monte_gb300 import abi
+    g, inp = mc_inputs(device)
+    prim = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device=device)
+    scat = torch.zeros_like(prim)
+    out = {"metric": "MC histories/s", "unit": "histories/s", "workload": MC_WORKLOAD}
+    stream = torch.cuda.current_stream(device)
+    for name, kernel in (("persistent", abi.MONTE_MC_PERSISTENT), ("plain", abi.MONTE_MC_PLAIN)):
+        req = abi.mc_request(2024, per, (0, 1), (0, g.nu), (0, g.nv), kernel)
+        st = ctx.mc_run(g, inp, req, prim, scat)  # warm-up
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        for i in range(steps):
+            req.view_begin, req.view_end = 1 + i, 2 + i
+            ctx.mc_run(g, inp, req, prim, scat)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        dt = e0.elapsed_time(e1) / 1e3
+        hist = steps * per * g.nu * g.nv
+        out[name] = {"value": hist / dt, "ms_per_view": dt / steps * 1e3,
+                     "woodcock_steps_per_history": st["woodcock_steps"] / st["histories"],
+                     "interactions_per_history": st["interactions"] / st["histories"]}
+    out["value"] = out["persistent"]["value"]
+    out["persistent_over_plain"] = out["persistent"]["value"] / out["plain"]["value"]
+    return out
+
+
 def run_reference(args):
     world, rank, local = dist_setup(args)
     if rank != 0:
@@ -224,6 +275,7 @@ def run_ours(args):
     bmode = abi.MONTE_BP_TILED if args.bp == "tiled" else abi.MONTE_BP_PLAIN
 
     proj = make_input(g, dev)
+    tile = ctx.fdk_autotune(g) if bmode == abi.MONTE_BP_TILED else -1
     filt = torch.empty((g.n_views, g.nv, g.nu), dtype=torch.float32, device=dev)
     vol = torch.empty((g.nz, g.ny, g.nx), dtype=torch.float32, device=dev)
     updates = g.nx * g.ny * g.nz * g.n_views
@@ -302,7 +354,9 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD if not args.small else "reduced (profiling) " + WORKLOAD,
                    "filter": {abi.MONTE_FILTER_FP32: "fp32", abi.MONTE_FILTER_BF16X3: "bf16x3"}[fmode],
-                   "backprojector": args.bp, "l2": "inputs 283 MB > 129 MB L2 (no flush)",
+                   "backprojector": args.bp, "bp_tile_variant": ctx.last_bp_variant(),
+                   "autotuned_tile": tile,
+                   "l2": "inputs 283 MB > 129 MB L2 (no flush)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "breakdown_ms": {"filter": t_filter * 1e3, "backprojection": t_bp * 1e3},
         "roofline": {"kernel": "backprojection", "bound": "fp32",
@@ -320,6 +374,28 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
+    # the plain one-instance FP32 form of the same FDK (FP32 filter, one voxel
+    # per thread backprojection), for the tuned-over-plain ratio
+    if not args.no_plain:
+        ctx.fdk(g, proj, vol, filtered=filt, filter_mode=abi.MONTE_FILTER_FP32,
+                bp_mode=abi.MONTE_BP_PLAIN)
+        torch.cuda.synchronize(dev)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        n_plain = 3
+        p0.record(stream)
+        for _ in range(n_plain):
+            ctx.fdk(g, proj, vol, filtered=filt, filter_mode=abi.MONTE_FILTER_FP32,
+                    bp_mode=abi.MONTE_BP_PLAIN)
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_plain = p0.elapsed_time(p1) / 1e3 / n_plain
+        line["fdk_plain"] = {"value": updates / t_plain / 1e9, "unit": "GUPS",
+                             "ms_per_step": t_plain * 1e3,
+                             "tuned_over_plain": value / world / (updates / t_plain / 1e9)}
+    if not args.no_mc:
+        line["mc"] = mc_bench(ctx, dev)
+        line["gpu_launches_mc"] = 2 * 4
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g)
     if rank == 0:

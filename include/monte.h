@@ -59,8 +59,11 @@ int monte_ctx_destroy(monte_ctx* ctx);
 /* Text of the last error raised on `ctx` (or of the last failed
  * monte_ctx_create when ctx is NULL). Never NULL. */
 const char* monte_last_error(const monte_ctx* ctx);
-/* Use a caller-provided cudaStream_t (NULL restores the context's own). */
+/* Queue the context's work on a caller-provided cudaStream_t; NULL means
+ * the CUDA legacy default stream (stream 0). */
 int monte_ctx_set_stream(monte_ctx* ctx, void* cuda_stream);
+/* Go back to the context's own non-blocking stream. */
+int monte_ctx_use_own_stream(monte_ctx* ctx);
 /* Wait for all work queued on the context's stream. */
 int monte_ctx_synchronize(monte_ctx* ctx);
 
@@ -141,6 +144,156 @@ int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* 
  * owned by the context is used instead).  recon/bp3d20.cpp:15-194. */
 int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
               float* vol_xy, float* vol_zy, int filter_mode, int bp_mode, int mem);
+
+/* Backprojection autotuner (no counterpart in the reference, whose
+ * backprojection is a fixed CPU loop nest, recon/bp3d20.cpp:83-166): times
+ * every tile shape (voxels per thread along z, columns per CTA, views per
+ * shared-memory stage) of MONTE_BP_TILED on geometry g and makes the fastest
+ * the context's choice for MONTE_BP_TILED.  *best receives its index, or -1
+ * if no tile shape fits g (MONTE_BP_TILED then runs the plain kernel). */
+int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best);
+/* Which kernel the last monte_fdk_backproject/monte_fdk call of this context
+ * ran: a tile shape index >= 0, or -1 for MONTE_BP_PLAIN. */
+int monte_fdk_last_bp_variant(const monte_ctx* ctx);
+/* Check the context's status word: MONTE_ETIMEOUT if a bounded wait inside
+ * a kernel gave up since the last check (the word is then cleared).
+ * Synchronizes the context's stream. */
+int monte_ctx_check_status(monte_ctx* ctx);
+
+/* ======================================================================
+ *  Monte Carlo
+ * ====================================================================== */
+
+/* Physics switches reproducing the reference programs' behaviour. */
+#define MONTE_MC_STALE_SIN_PHI     0x1 /* a 2nd or later Compton rotates from the
+                                          emission sin_phi_a, which the GPU program
+                                          never refreshes (monte_cu/CBCT_real325im.cu:768-773) */
+#define MONTE_MC_FIRST_COMPTON_Z   0x2 /* the first Compton turns about +z: the CPU
+                                          program starts from sin_theta_a_new = 0
+                                          (monte_cpp/CBCT_real2.cpp:193,460-463) */
+#define MONTE_MC_NO_RAYLEIGH_TALLY 0x4 /* photons whose last interaction was Rayleigh
+                                          are not tallied (monte_cpp/CBCT_real2.cpp:373-397) */
+
+/* Kernels. */
+#define MONTE_MC_PLAIN      0 /* one thread per emitting pixel, histories in sequence
+                                 (the reference's launch shape, CBCT_real325im.cu:462-464) */
+#define MONTE_MC_PERSISTENT 1 /* persistent warps that refill lanes as histories end */
+
+/*
+ * Acquisition geometry of the Monte Carlo.  Replaces the #defines and
+ * constants of monte_cu/CBCT_real325im.cu:6-18,459-460 and
+ * monte_cpp/CBCT_real2.cpp:8-9,205-254.  The source sits at (-sod, 0, 0)
+ * rotated by the view angle k*360/n_views degrees about z; the detector
+ * plane is at distance sdd from the source.  Pixel (i, j) of a view is
+ * centred at u = half_u - du*(i+0.5) (in-plane) and v = half_v - dv*(j+0.5)
+ * (axial); every history of pixel (i, j) is aimed at that centre
+ * (CBCT_real325im.cu:476-512).  Photons start on the plane x' = -start_plane
+ * of the view frame (:522-540).
+ */
+typedef struct monte_mc_geom {
+  int32_t n_views;
+  int32_t nu, nv;           /* detector pixels (in-plane, axial) */
+  int32_t max_interactions; /* interactions followed per history (ScatterNUM) */
+  uint32_t flags;           /* MONTE_MC_* */
+  int32_t reserved0;
+  double du, dv, half_u, half_v;
+  double sod, sdd;
+  double start_plane;
+} monte_mc_geom;
+
+/*
+ * Label-volume phantom, labels[nz][ny][nx] (uint8), voxel (ix,iy,iz)
+ * covering x in [x0 + ix*dx, x0 + (ix+1)*dx) etc. (CBCT_real325im.cu:921:
+ * x0 = y0 = z0 = -10 cm, d = 0.1 cm).  Label l is material label_material[l]
+ * (an index into the XCOM tables, or -1 for air) at density
+ * label_density[l] g/cm^3.  If clip_radius > 0, labels outside the cylinder
+ * x^2+y^2 <= clip_radius^2, |z| <= clip_half_z read as air (:904).
+ * `labels` follows the call's `mem`; the two label tables are host memory.
+ */
+typedef struct monte_mc_phantom {
+  const uint8_t* labels;
+  int32_t nx, ny, nz;
+  int32_t n_labels;         /* <= 256 */
+  double dx, dy, dz;
+  double x0, y0, z0;
+  double clip_radius, clip_half_z;
+  const int32_t* label_material;
+  const double* label_density;
+} monte_mc_phantom;
+
+/* XCOM mass coefficients [cm^2/g] per material, each [n_materials][201]
+ * indexed by keV (row r of the reference CSV at index r,
+ * monte_cpp/CBCT_real2.cpp:633-668).  Host memory. */
+typedef struct monte_xcom {
+  int32_t n_materials;      /* <= 8 */
+  int32_t reserved0;
+  const float* coherent;
+  const float* incoherent;
+  const float* photoelectric;
+  const float* total;
+} monte_xcom;
+
+/* Source spectrum: discrete lines with relative weights (a single line is
+ * monoenergetic; the reference forces 140 keV, CBCT_real325im.cu:491).
+ * Host memory. */
+typedef struct monte_spectrum {
+  int32_t n_lines;          /* 1..512 */
+  int32_t reserved0;
+  const double* energy_kev;
+  const double* weight;
+} monte_spectrum;
+
+/* What to simulate: `histories_per_pixel` histories aimed at every pixel
+ * of [u_begin,u_end) x [v_begin,v_end) for every view of
+ * [view_begin,view_end).  History k of (view, i, j) draws from the stream
+ * ((view*nu + i)*nv + j)*histories_per_pixel + k of seed `seed`, job `job`,
+ * so any split of the work reproduces the same tallies. */
+typedef struct monte_mc_request {
+  uint64_t seed;
+  uint64_t histories_per_pixel;
+  int32_t view_begin, view_end;
+  int32_t u_begin, u_end, v_begin, v_end;
+  int32_t kernel;           /* MONTE_MC_PLAIN / MONTE_MC_PERSISTENT */
+  uint32_t job;
+} monte_mc_request;
+
+typedef struct monte_mc_stats {
+  uint64_t histories;
+  uint64_t woodcock_steps;
+  uint64_t interactions;
+  uint64_t primary_counts;  /* tallied */
+  uint64_t scatter_counts;  /* tallied */
+  uint64_t dropped;         /* histories stopped by a step or rejection cap */
+} monte_mc_stats;
+
+/* Defaults equal to monte_cu/CBCT_real325im.cu: 360 views, 325x325 pixels
+ * of 0.1 cm, SOD 160, SDD 220, start plane 10.1, 5 interactions,
+ * MONTE_MC_STALE_SIN_PHI. */
+void monte_mc_geom_reference325(monte_mc_geom* g);
+/* Defaults equal to monte_cpp/CBCT_real2.cpp: 65x65 pixels of 0.5 cm, start
+ * plane 6, 5 interactions, MONTE_MC_FIRST_COMPTON_Z | MONTE_MC_NO_RAYLEIGH_TALLY. */
+void monte_mc_geom_reference_cpu(monte_mc_geom* g);
+
+/* Parse one XCOM CSV (rows "coh,incoh,photo,total", UTF-8 BOM and CRLF
+ * tolerated) into four [201] arrays indexed by keV.  Host only, no GPU. */
+int monte_xcom_parse_csv(const char* text, size_t len, float* coherent, float* incoherent,
+                         float* photoelectric, float* total);
+
+/* Run the Monte Carlo.  primary and scatter are int64 [n_views][nu][nv]
+ * tallies that the call ADDS to (zero them first); they follow `mem`.
+ * stats may be NULL.  Replaces the projection launch of
+ * monte_cu/CBCT_real325im.cu:235-248. */
+int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom* ph,
+                 const monte_xcom* xcom, const monte_spectrum* spec, const monte_mc_request* run,
+                 int64_t* primary, int64_t* scatter, monte_mc_stats* stats, int mem);
+
+/* Reference post-processing (monte_cu/CBCT_real325im.cu:261-294): counts
+ * clamped to [1, per]; map = -ln N + ln(per).  proj0/map0 from the primary
+ * tally, proj5/map5 from primary + scatter; any output may be NULL.  All
+ * arrays [n_views][nu][nv], following `mem`. */
+int monte_mc_finalize(monte_ctx* ctx, int32_t n_views, int32_t nu, int32_t nv, uint64_t per,
+                      const int64_t* primary, const int64_t* scatter, int32_t* proj0,
+                      float* map0, int32_t* proj5, float* map5, int mem);
 
 #ifdef __cplusplus
 }

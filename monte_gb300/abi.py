@@ -94,6 +94,201 @@ def fdk_geom_reference325():
     return g
 
 
+MONTE_MC_STALE_SIN_PHI = 0x1
+MONTE_MC_FIRST_COMPTON_Z = 0x2
+MONTE_MC_NO_RAYLEIGH_TALLY = 0x4
+MONTE_MC_PLAIN = 0
+MONTE_MC_PERSISTENT = 1
+
+
+class McGeom(C.Structure):
+    """monte_mc_geom."""
+
+    _fields_ = [
+        ("n_views", C.c_int32),
+        ("nu", C.c_int32),
+        ("nv", C.c_int32),
+        ("max_interactions", C.c_int32),
+        ("flags", C.c_uint32),
+        ("reserved0", C.c_int32),
+        ("du", C.c_double),
+        ("dv", C.c_double),
+        ("half_u", C.c_double),
+        ("half_v", C.c_double),
+        ("sod", C.c_double),
+        ("sdd", C.c_double),
+        ("start_plane", C.c_double),
+    ]
+
+
+class McPhantom(C.Structure):
+    """monte_mc_phantom (keeps references to the arrays it points at)."""
+
+    _fields_ = [
+        ("labels", C.c_void_p),
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("nz", C.c_int32),
+        ("n_labels", C.c_int32),
+        ("dx", C.c_double),
+        ("dy", C.c_double),
+        ("dz", C.c_double),
+        ("x0", C.c_double),
+        ("y0", C.c_double),
+        ("z0", C.c_double),
+        ("clip_radius", C.c_double),
+        ("clip_half_z", C.c_double),
+        ("label_material", C.POINTER(C.c_int32)),
+        ("label_density", C.POINTER(C.c_double)),
+    ]
+
+
+class McXcom(C.Structure):
+    """monte_xcom."""
+
+    _fields_ = [
+        ("n_materials", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("coherent", C.POINTER(C.c_float)),
+        ("incoherent", C.POINTER(C.c_float)),
+        ("photoelectric", C.POINTER(C.c_float)),
+        ("total", C.POINTER(C.c_float)),
+    ]
+
+
+class McSpectrum(C.Structure):
+    """monte_spectrum."""
+
+    _fields_ = [
+        ("n_lines", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("energy_kev", C.POINTER(C.c_double)),
+        ("weight", C.POINTER(C.c_double)),
+    ]
+
+
+class McRequest(C.Structure):
+    """monte_mc_request."""
+
+    _fields_ = [
+        ("seed", C.c_uint64),
+        ("histories_per_pixel", C.c_uint64),
+        ("view_begin", C.c_int32),
+        ("view_end", C.c_int32),
+        ("u_begin", C.c_int32),
+        ("u_end", C.c_int32),
+        ("v_begin", C.c_int32),
+        ("v_end", C.c_int32),
+        ("kernel", C.c_int32),
+        ("job", C.c_uint32),
+    ]
+
+
+class McStats(C.Structure):
+    """monte_mc_stats."""
+
+    _fields_ = [(n, C.c_uint64) for n in ("histories", "woodcock_steps", "interactions",
+                                          "primary_counts", "scatter_counts", "dropped")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+def mc_geom_reference325():
+    """monte_cu/CBCT_real325im.cu: 360 views, 325x325 pixels of 0.1 cm, SOD 160,
+    SDD 220, start plane 10.1, 5 interactions, the stale sin_phi_a quirk."""
+    g = McGeom()
+    g.n_views, g.nu, g.nv = 360, 325, 325
+    g.max_interactions = 5
+    g.flags = MONTE_MC_STALE_SIN_PHI
+    g.du = g.dv = 0.1
+    g.half_u = g.half_v = 16.25
+    g.sod, g.sdd, g.start_plane = 160.0, 220.0, 10.1
+    return g
+
+
+def mc_geom_reference_cpu():
+    """monte_cpp/CBCT_real2.cpp: 65x65 pixels of 0.5 cm, start plane 6, first
+    Compton about +z, no tally after Rayleigh."""
+    g = McGeom()
+    g.n_views, g.nu, g.nv = 360, 65, 65
+    g.max_interactions = 5
+    g.flags = MONTE_MC_FIRST_COMPTON_Z | MONTE_MC_NO_RAYLEIGH_TALLY
+    g.du = g.dv = 0.5
+    g.half_u = g.half_v = 16.25
+    g.sod, g.sdd, g.start_plane = 160.0, 220.0, 6.0
+    return g
+
+
+def mc_geom(n_views, nu, nv, pitch_cm, sod_cm, sdd_cm, start_plane_cm, flags=0,
+            max_interactions=5):
+    g = McGeom()
+    g.n_views, g.nu, g.nv = n_views, nu, nv
+    g.max_interactions = max_interactions
+    g.flags = flags
+    g.du = g.dv = pitch_cm
+    g.half_u = nu * pitch_cm / 2.0
+    g.half_v = nv * pitch_cm / 2.0
+    g.sod, g.sdd, g.start_plane = sod_cm, sdd_cm, start_plane_cm
+    return g
+
+
+class McInputs:
+    """Host-side bundle of the phantom/XCOM/spectrum structs and the arrays
+    they point at (kept alive here).  `labels` may be a numpy array (host)
+    or a torch CUDA tensor (device)."""
+
+    def __init__(self, labels, voxel_cm, origin_cm, label_material, label_density,
+                 xcom_tables, energies_kev, weights=None, clip_radius=0.0, clip_half_z=0.0):
+        import numpy as np
+        self.labels = labels
+        nz, ny, nx = labels.shape
+        self.mat = np.ascontiguousarray(label_material, np.int32)
+        self.rho = np.ascontiguousarray(label_density, np.float64)
+        ph = McPhantom()
+        ph.labels = labels.data_ptr() if hasattr(labels, "data_ptr") else labels.ctypes.data
+        ph.nx, ph.ny, ph.nz = nx, ny, nz
+        ph.n_labels = len(self.mat)
+        ph.dx, ph.dy, ph.dz = voxel_cm if hasattr(voxel_cm, "__len__") else (voxel_cm,) * 3
+        ph.x0, ph.y0, ph.z0 = origin_cm
+        ph.clip_radius, ph.clip_half_z = clip_radius, clip_half_z
+        ph.label_material = self.mat.ctypes.data_as(C.POINTER(C.c_int32))
+        ph.label_density = self.rho.ctypes.data_as(C.POINTER(C.c_double))
+        self.phantom = ph
+        # xcom_tables: list of [4][201] arrays (coh, incoh, photo, total)
+        tabs = np.ascontiguousarray(np.stack(xcom_tables), np.float32)  # [m][4][201]
+        self.coh = np.ascontiguousarray(tabs[:, 0, :])
+        self.inc = np.ascontiguousarray(tabs[:, 1, :])
+        self.pho = np.ascontiguousarray(tabs[:, 2, :])
+        self.tot = np.ascontiguousarray(tabs[:, 3, :])
+        x = McXcom()
+        x.n_materials = tabs.shape[0]
+        fp = C.POINTER(C.c_float)
+        x.coherent = self.coh.ctypes.data_as(fp)
+        x.incoherent = self.inc.ctypes.data_as(fp)
+        x.photoelectric = self.pho.ctypes.data_as(fp)
+        x.total = self.tot.ctypes.data_as(fp)
+        self.xcom = x
+        self.E = np.ascontiguousarray(np.atleast_1d(energies_kev), np.float64)
+        self.W = np.ascontiguousarray(np.ones_like(self.E) if weights is None else weights,
+                                      np.float64)
+        s = McSpectrum()
+        s.n_lines = len(self.E)
+        s.energy_kev = self.E.ctypes.data_as(C.POINTER(C.c_double))
+        s.weight = self.W.ctypes.data_as(C.POINTER(C.c_double))
+        self.spectrum = s
+
+
+def mc_request(seed, per, views, u_range, v_range, kernel=MONTE_MC_PERSISTENT, job=0):
+    r = McRequest()
+    r.seed, r.histories_per_pixel = seed, per
+    r.view_begin, r.view_end = views
+    r.u_begin, r.u_end = u_range
+    r.v_begin, r.v_end = v_range
+    r.kernel, r.job = kernel, job
+    return r
+
+
 def fdk_geom_recon325(n_views=360, nu=512, nv=384, pitch_mm=0.8, sod_mm=500.0,
                       sdd_mm=1000.0, n=325, voxel_mm=0.4):
     """FDK at the recon-325 workload: 360 views of a 512 (in-plane) x 384

@@ -124,6 +124,7 @@ int monte_ctx_destroy(monte_ctx* ctx) {
   if (ctx->stream && ctx->stream != ctx->own_stream) cudaStreamSynchronize(ctx->stream);
   for (auto& b : ctx->scratch) monte::release(b);
   monte::release(ctx->fdk_views);
+  monte::release(ctx->fdk_viewsd);
   monte::release(ctx->fdk_weights);
   monte::release(ctx->fdk_taps);
   monte::release(ctx->fdk_bsplit);
@@ -146,13 +147,36 @@ const char* monte_last_error(const monte_ctx* ctx) {
 
 int monte_ctx_set_stream(monte_ctx* ctx, void* cuda_stream) {
   if (!ctx) return MONTE_EINVAL;
-  ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+  ctx->stream = (cudaStream_t)cuda_stream;
+  return MONTE_OK;
+}
+
+int monte_ctx_use_own_stream(monte_ctx* ctx) {
+  if (!ctx) return MONTE_EINVAL;
+  ctx->stream = ctx->own_stream;
   return MONTE_OK;
 }
 
 int monte_ctx_synchronize(monte_ctx* ctx) {
   MONTE_TRY(monte::enter(ctx));
   MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MONTE_OK;
+}
+
+int monte_ctx_check_status(monte_ctx* ctx) {
+  MONTE_TRY(monte::enter(ctx));
+  int h = 0;
+  MONTE_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h != 0) {
+    MONTE_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+    MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return monte::set_error(ctx, MONTE_ETIMEOUT,
+                            "a bounded device wait gave up (kernel status %d); results of the "
+                            "affected launch are invalid",
+                            h);
+  }
   return MONTE_OK;
 }
 

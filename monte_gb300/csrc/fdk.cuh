@@ -20,15 +20,25 @@ struct BpView {
   float pad;
 };
 
-// Geometry as the kernels use it (float), derived from monte_fdk_geom.
+// The same per-view constants in double, for re-evaluating voxel-view pairs
+// that sit on a discontinuity of the reference's operator (see
+// bp_ref_voxel below).
+struct BpViewD {
+  double c, s, px, py, tanb;
+};
+
+// Geometry as the kernels use it (float), derived from monte_fdk_geom, plus
+// the double originals used by bp_ref_voxel.
 struct FdkDev {
+  double x0d, y0d, z0d, dvoxd, sddd, Dd;
+  double half_ud, half_vd, inv_dud, inv_dvd;
   int n_views, nu, nv, nx, ny, nz;
   int s_begin, s_end;
   int mask_r2;           // <=0: no mask
   int cs, ct, cz;        // mask centre
   int flags;
   float x0, y0, z0, dvox;
-  float sdd, D;
+  float sdd, D, sod;
   float half_u, half_v;
   float inv_du, inv_dv;
   float xmax, ymax;      // accepted detector coordinate ranges [0,xmax], [0,ymax]
@@ -48,10 +58,13 @@ size_t bf16x3_bsplit_bytes(int nu);
 void bf16x3_build_bsplit(int nu, const float* taps_half, uint16_t* out);
 bool bf16x3_supported(const FdkDev& d);
 
-cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const float* filtered,
-                                float* vol_xy, float* vol_zy, cudaStream_t st);
-cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const float* filtered,
-                                float* vol_xy, float* vol_zy, int variant, cudaStream_t st);
+cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
+                                const float* filtered, float* vol_xy, float* vol_zy,
+                                cudaStream_t st);
+// status: device int set to 1 if a bounded wait gave up (MONTE_ETIMEOUT)
+cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
+                                const float* filtered, float* vol_xy, float* vol_zy,
+                                int variant, int* status, cudaStream_t st);
 int fdk_bp_tiled_variants();
 bool fdk_bp_tiled_supported(const FdkDev& d, int variant);
 
@@ -78,6 +91,65 @@ __device__ __forceinline__ float bp_bilinear_global(const FdkDev& d, const float
   float r0 = fmaf(fx, f10 - f00, f00);
   float r1 = fmaf(fx, f11 - f01, f01);
   return fmaf(fy, r1 - r0, r0);
+}
+
+// Bilinear read at double coordinates (the weights rounded to float).
+__device__ __forceinline__ float bp_bilinear_global_d(const FdkDev& d, const float* __restrict__ f,
+                                                      int k, double x, double y) {
+  const size_t total = (size_t)d.n_views * d.nu * d.nv;
+  int xi = (int)x, yi = (int)y;
+  float fx = (float)(x - xi), fy = (float)(y - yi);
+  size_t i00 = (size_t)k * d.nu * d.nv + (size_t)xi * d.nu + yi;
+  bool flat = (d.flags & MONTE_FDK_FLAT_EDGE) != 0;
+  float f00 = bp_fetch(f, total, i00, flat || (xi < d.nv && yi < d.nu));
+  float f10 = bp_fetch(f, total, i00 + d.nu, flat || (xi + 1 < d.nv && yi < d.nu));
+  float f01 = bp_fetch(f, total, i00 + 1, flat || (xi < d.nv && yi + 1 < d.nu));
+  float f11 = bp_fetch(f, total, i00 + d.nu + 1, flat || (xi + 1 < d.nv && yi + 1 < d.nu));
+  float r0 = fmaf(fx, f10 - f00, f00);
+  float r1 = fmaf(fx, f11 - f01, f01);
+  return fmaf(fy, r1 - r0, r0);
+}
+
+// One voxel-view pair evaluated in double exactly as recon/bp3d20.cpp:95-142
+// does (same operations, same order, no contraction): whether the voxel is
+// rejected (:116), its detector coordinates x, y (:123-124 /
+// bp3d20_325.cpp:134-135) and the distance weight D^2/(D-d)^2 (:134-142,159).
+// The reference's operator jumps where tmp_s changes sign (the weight, when
+// tan() is evaluated as the reference does) and at the detector edges, so
+// pairs the float path finds within a small margin of those places are
+// decided here.  Returns false when rejected.
+__device__ __forceinline__ bool bp_ref_voxel(const FdkDev& d, const BpViewD& v, int s, int t,
+                                             int z, double* x, double* y, double* w) {
+  double X = __dadd_rn(d.x0d, __dmul_rn((double)s, d.dvoxd));
+  double Y = __dsub_rn(d.y0d, __dmul_rn((double)t, d.dvoxd));
+  double Z = __dsub_rn(d.z0d, __dmul_rn((double)z, d.dvoxd));
+  double p0 = __dsub_rn(X, v.px), p1 = __dsub_rn(Y, v.py), p2 = Z;
+  double tmp = p0;
+  p0 = __dadd_rn(__dmul_rn(p0, v.c), __dmul_rn(p1, v.s));
+  p1 = __dadd_rn(-__dmul_rn(tmp, v.s), __dmul_rn(p1, v.c));
+  double to = __ddiv_rn(d.sddd, p0);
+  p1 = __dmul_rn(p1, to);
+  p2 = __dmul_rn(p2, to);
+  if (fabs(p1) > d.half_ud || fabs(p2) > d.half_vd) return false;
+  *y = -__dsub_rn(__dmul_rn(p1, d.inv_dud), __dmul_rn(d.half_ud, d.inv_dud));
+  *x = -__dsub_rn(__dmul_rn(p2, d.inv_dvd), __dmul_rn(d.half_vd, d.inv_dvd));
+  double ts = __dsub_rn(__dmul_rn(X, v.c), __dmul_rn(Y, v.s));
+  double tt = __dadd_rn(__dmul_rn(X, v.s), __dmul_rn(Y, v.c));
+  double dd = fabs(__dadd_rn(-__dmul_rn(v.tanb, tt), ts)) /
+              __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(v.tanb, v.tanb)));
+  if (ts < 0) dd = -dd;
+  double den = __dsub_rn(d.Dd, dd);
+  *w = __ddiv_rn(__dmul_rn(d.Dd, d.Dd), __dmul_rn(den, den));
+  return true;
+}
+
+// Whether a float-path evaluation is close enough to a discontinuity of the
+// reference operator that it must be re-decided in double.
+__device__ __forceinline__ bool bp_near_edge(const FdkDev& d, float ts, float up, float vp, float x,
+                                             float y) {
+  return fabsf(ts) < 1e-4f || fabsf(fabsf(up) - d.half_u) < 1e-4f * d.half_u ||
+         fabsf(fabsf(vp) - d.half_v) < 1e-4f * d.half_v || fabsf(x - d.xmax) < 1e-3f ||
+         fabsf(y - d.ymax) < 1e-3f || fabsf(x) < 1e-3f || fabsf(y) < 1e-3f;
 }
 
 #endif

@@ -17,6 +17,16 @@ namespace monte {
 
 FdkDev make_fdk_dev(const monte_fdk_geom& g) {
   FdkDev d;
+  d.x0d = g.x0;
+  d.y0d = g.y0;
+  d.z0d = g.z0;
+  d.dvoxd = g.dvox;
+  d.sddd = g.sdd;
+  d.Dd = g.wdist;
+  d.half_ud = g.half_u;
+  d.half_vd = g.half_v;
+  d.inv_dud = 1.0 / g.du;
+  d.inv_dvd = 1.0 / g.dv;
   d.n_views = g.n_views;
   d.nu = g.nu;
   d.nv = g.nv;
@@ -36,6 +46,7 @@ FdkDev make_fdk_dev(const monte_fdk_geom& g) {
   d.dvox = (float)g.dvox;
   d.sdd = (float)g.sdd;
   d.D = (float)g.wdist;
+  d.sod = (float)g.sod;
   d.half_u = (float)g.half_u;
   d.half_v = (float)g.half_v;
   d.inv_du = (float)(1.0 / g.du);
@@ -86,6 +97,7 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
   if (key == ctx->fdk_key && ctx->fdk_views.ptr) return MONTE_OK;
   const int nv_ = g->n_views, nu = g->nu, nv = g->nv;
   std::vector<BpView> views(nv_);
+  std::vector<BpViewD> viewsd(nv_);
   float beta_span = (float)(360.0 / nv_);
   for (int k = 0; k < nv_; k++) {
     double beta = (double)k * 360.0 / nv_;
@@ -102,6 +114,11 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
     v.rs = (float)(1.0 / sqrt(1 + tanb * tanb));
     v.factor = (float)(beta_span * 2 * M_PI / 360 * g->scale * g->scale2);
     v.pad = 0.f;
+    viewsd[k].c = c;
+    viewsd[k].s = s;
+    viewsd[k].px = start_x * c - 0.f * s;  // recon/bp3d20.cpp:87-88
+    viewsd[k].py = start_x * s + 0.f * c;
+    viewsd[k].tanb = tanb;
   }
   // cosine weights w[u][v] (recon/bp3d20.cpp:40)
   std::vector<float> w((size_t)nu * nv);
@@ -124,6 +141,10 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
     taps[nu - 1 + n] = taps[nu - 1 - n] = 0.5f * h;
   }
   MONTE_TRY(ensure(ctx, ctx->fdk_views, views.size() * sizeof(BpView), "view table"));
+  MONTE_TRY(ensure(ctx, ctx->fdk_viewsd, viewsd.size() * sizeof(BpViewD), "view table"));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_viewsd.ptr, viewsd.data(),
+                                  viewsd.size() * sizeof(BpViewD), cudaMemcpyHostToDevice,
+                                  ctx->stream));
   MONTE_TRY(ensure(ctx, ctx->fdk_weights, w.size() * sizeof(float), "weight table"));
   MONTE_TRY(ensure(ctx, ctx->fdk_taps, taps.size() * sizeof(float), "tap table"));
   MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_views.ptr, views.data(), views.size() * sizeof(BpView),
@@ -177,15 +198,22 @@ int run_bp(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_filtered, flo
   }
   cudaError_t e;
   const BpView* views = (const BpView*)ctx->fdk_views.ptr;
+  const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
   if (bp_mode == MONTE_BP_PLAIN) {
-    e = launch_fdk_bp_plain(d, views, d_filtered, d_xy, d_zy, ctx->stream);
+    e = launch_fdk_bp_plain(d, views, viewsd, d_filtered, d_xy, d_zy, ctx->stream);
+    ctx->last_bp_variant = -1;
   } else if (bp_mode == MONTE_BP_TILED) {
     int variant = ctx->bp_tune_choice;
     if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
     if (!fdk_bp_tiled_supported(d, variant)) {
-      e = launch_fdk_bp_plain(d, views, d_filtered, d_xy, d_zy, ctx->stream);
+      // the footprint of a voxel block does not fit a shared-memory box:
+      // the one-voxel-per-thread kernel handles any geometry
+      e = launch_fdk_bp_plain(d, views, viewsd, d_filtered, d_xy, d_zy, ctx->stream);
+      ctx->last_bp_variant = -1;
     } else {
-      e = launch_fdk_bp_tiled(d, views, d_filtered, d_xy, d_zy, variant, ctx->stream);
+      e = launch_fdk_bp_tiled(d, views, viewsd, d_filtered, d_xy, d_zy, variant, ctx->d_status,
+                              ctx->stream);
+      ctx->last_bp_variant = variant;
     }
   } else {
     return set_error(ctx, MONTE_EINVAL, "unknown backprojection mode %d", bp_mode);
@@ -325,5 +353,55 @@ int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float*
   MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return MONTE_OK;
 }
+
+int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
+  if (!ctx) return MONTE_EINVAL;
+  MONTE_TRY(validate(ctx, g, true));
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(prepare_tables(ctx, g));
+  FdkDev d = make_fdk_dev(*g);
+  const size_t pb = proj_bytes(g), vb = vol_bytes(g);
+  MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "autotune filtered"));
+  MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "autotune volume"));
+  MONTE_CUDA(ctx, cudaMemsetAsync(ctx->scratch[kScratchFiltered].ptr, 0, pb, ctx->stream));
+  const float* df = (const float*)ctx->scratch[kScratchFiltered].ptr;
+  float* dv = (float*)ctx->scratch[kScratchVolXY].ptr;
+  const BpView* views = (const BpView*)ctx->fdk_views.ptr;
+  const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
+  cudaEvent_t e0, e1;
+  MONTE_CUDA(ctx, cudaEventCreate(&e0));
+  MONTE_CUDA(ctx, cudaEventCreate(&e1));
+  int pick = -1;
+  float best_ms = 3.0e38f;
+  for (int v = 0; v < fdk_bp_tiled_variants(); v++) {
+    if (!fdk_bp_tiled_supported(d, v)) continue;
+    float ms_min = 3.0e38f;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, ctx->stream);
+      cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, dv, nullptr, v, ctx->d_status,
+                                          ctx->stream);
+      cudaEventRecord(e1, ctx->stream);
+      if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(ctx, e != cudaSuccess ? e : cudaGetLastError(), "autotune launch");
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0 && ms < ms_min) ms_min = ms;  // first run warms up
+    }
+    if (ms_min < best_ms) {
+      best_ms = ms_min;
+      pick = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->bp_tune_choice = pick;
+  if (best) *best = pick;
+  return monte_ctx_check_status(ctx);
+}
+
+int monte_fdk_last_bp_variant(const monte_ctx* ctx) { return ctx ? ctx->last_bp_variant : -1; }
 
 }  // extern "C"

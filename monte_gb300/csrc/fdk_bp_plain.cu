@@ -14,6 +14,7 @@ namespace monte {
 namespace {
 
 __global__ void __launch_bounds__(256) bp_plain_kernel(FdkDev d, const BpView* __restrict__ views,
+                                                       const BpViewD* __restrict__ viewsd,
                                                        const float* __restrict__ filtered,
                                                        float* __restrict__ vol_xy,
                                                        float* __restrict__ vol_zy) {
@@ -41,18 +42,26 @@ __global__ void __launch_bounds__(256) bp_plain_kernel(FdkDev d, const BpView* _
       float Vy = ay * v.c - ax * v.s;
       float kk = d.sdd / Vx;
       float up = Vy * kk, vp = Z * kk;
-      if (fabsf(up) > d.half_u || fabsf(vp) > d.half_v) continue;
       float y = (d.half_u - up) * d.inv_du;
       float x = (d.half_v - vp) * d.inv_dv;
-      float val = 0.f;
-      if (x >= 0.f && x <= d.xmax && y >= 0.f && y <= d.ymax)
-        val = bp_bilinear_global(d, filtered, k, x, y);
       float ts = X * v.c - Y * v.s;
-      float tt = X * v.s + Y * v.c;
-      float dd = fabsf(ts - v.tanb * tt) * v.rs;
-      if (ts < 0.f) dd = -dd;
-      float den = d.D - dd;
-      float w = (d.D * d.D) / (den * den);
+      float w, val = 0.f;
+      if (!bp_near_edge(d, ts, up, vp, x, y)) {
+        if (fabsf(up) > d.half_u || fabsf(vp) > d.half_v) continue;  // recon/bp3d20.cpp:116
+        if (x >= 0.f && x <= d.xmax && y >= 0.f && y <= d.ymax)
+          val = bp_bilinear_global(d, filtered, k, x, y);
+        float tt = X * v.s + Y * v.c;
+        float dd = fabsf(ts - v.tanb * tt) * v.rs;
+        if (ts < 0.f) dd = -dd;
+        float den = d.D - dd;
+        w = (d.D * d.D) / (den * den);
+      } else {
+        double xd, yd, wd;
+        if (!bp_ref_voxel(d, viewsd[k], s, t, z, &xd, &yd, &wd)) continue;
+        if (xd >= 0.0 && xd <= (double)d.nv && yd >= 0.0 && yd <= (double)d.nu)
+          val = bp_bilinear_global_d(d, filtered, k, xd, yd);
+        w = (float)wd;
+      }
       acc = fmaf(w * val, v.factor, acc);
     }
   }
@@ -62,12 +71,13 @@ __global__ void __launch_bounds__(256) bp_plain_kernel(FdkDev d, const BpView* _
 
 }  // namespace
 
-cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const float* filtered,
-                                float* vol_xy, float* vol_zy, cudaStream_t st) {
+cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
+                                const float* filtered, float* vol_xy, float* vol_zy,
+                                cudaStream_t st) {
   const size_t n_vox = (size_t)(d.s_end - d.s_begin) * d.ny * d.nz;
   if (n_vox == 0) return cudaSuccess;
   unsigned blocks = (unsigned)((n_vox + 255) / 256);
-  bp_plain_kernel<<<blocks, 256, 0, st>>>(d, views, filtered, vol_xy, vol_zy);
+  bp_plain_kernel<<<blocks, 256, 0, st>>>(d, views, viewsd, filtered, vol_xy, vol_zy);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,230 @@
+// mc_kernels.cu -- photon-history Monte Carlo kernels for sm_103a.
+//
+// Reference kernel: `projection` of monte_cu/CBCT_real325im.cu:425-860 --
+// one thread per detector pixel runs every view and every history of that
+// pixel in sequence, so a warp waits for its longest history at every
+// history boundary (a primary ends after one flight, a scattered photon
+// after up to five interactions and hundreds of Woodcock steps).
+//
+//  * mc_plain_kernel: the same launch shape (one thread per emitting pixel,
+//    views x histories in sequence), the FP32 one-instance baseline.
+//  * mc_persistent_kernel: persistent warps over a global history counter.
+//    A lane whose photon ends takes the next history at once: the warp
+//    ballots its idle lanes, ranks them with popc and hands them
+//    consecutive history ids from a per-warp chunk claimed with one atomic.
+//    Flights advance a few Woodcock steps per round; lanes that reach a
+//    real collision wait until enough of the warp has one (or no lane is
+//    flying), so the divergent interaction code runs on a compacted set.
+//    Tallies are warp-aggregated: lanes that hit the same pixel are grouped
+//    with __match_any_sync and one leader adds the group's count.
+//  * mc_finalize_kernel: the reference's host post-processing
+//    (CBCT_real325im.cu:261-294) -- clamp, then -ln N + ln per in FP64.
+//
+// Every history draws from its own Philox stream (monte_rng.h) and runs the
+// step functions of mc_physics.h, so both kernels produce bit-identical
+// int64 tallies, equal to the CPU replay harness's.
+#include <cuda_runtime.h>
+
+#include "mc.cuh"
+
+namespace monte {
+
+namespace {
+
+constexpr int kChunk = 64;          // histories claimed per warp atomic
+constexpr int kStepsPerRound = 4;   // Woodcock steps per flight per round
+constexpr int kCollideBatch = 12;   // interact once this many lanes wait
+
+__device__ __forceinline__ void decompose(const McDev& d, unsigned long long h, int* view,
+                                          int* iu, int* iv, unsigned long long* k) {
+  const unsigned long long per = d.P.per;
+  const unsigned nv_roi = (unsigned)(d.P.v_end - d.P.v_begin);
+  const unsigned nu_roi = (unsigned)(d.P.u_end - d.P.u_begin);
+  unsigned long long rest = h / per;
+  *k = h - rest * per;
+  unsigned long long npix = (unsigned long long)nu_roi * nv_roi;
+  unsigned long long vw = rest / npix;
+  unsigned pix = (unsigned)(rest - vw * npix);
+  *view = d.P.view_begin + (int)vw;
+  *iu = d.P.u_begin + (int)(pix / nv_roi);
+  *iv = d.P.v_begin + (int)(pix % nv_roi);
+}
+
+__device__ __forceinline__ void warp_stats(const McDev& d, unsigned long long v[6]) {
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    unsigned long long x = v[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(&d.stats[i], x);
+  }
+}
+
+__global__ void __launch_bounds__(128) mc_plain_kernel(McDev d) {
+  const int nv_roi = d.P.v_end - d.P.v_begin;
+  const int nu_roi = d.P.u_end - d.P.u_begin;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
+  if (idx < nu_roi * nv_roi) {
+    const int iu = d.P.u_begin + idx / nv_roi;
+    const int iv = d.P.v_begin + idx % nv_roi;
+    for (int view = d.P.view_begin; view < d.P.view_end; view++) {
+      for (unsigned long long k = 0; k < d.P.per; k++) {
+        mc_photon p;
+        mc_start(&d.P, d.T, d.V, d.U, d.W, view, iu, iv, k, &p);
+        st[0]++;
+        while (true) {
+          if (p.state == MC_FLY) {
+            mc_flight_step(&d.P, d.T, d.labels, &p);
+            st[1]++;
+            if (p.state == MC_DEAD) st[5]++;
+          } else if (p.state == MC_COLLIDED) {
+            p.state = mc_after_collision(&d.P, d.T, &p);
+          } else if (p.state == MC_ESCAPED) {
+            int kind = mc_tally_kind(&d.P, &p);
+            long long cell = mc_detector_index(&d.P, d.V, &p);
+            if (kind >= 0 && cell >= 0) {
+              atomicAdd(kind == 0 ? &d.prim[cell] : &d.scat[cell], 1ull);
+              st[3 + kind]++;
+            }
+            break;
+          } else {
+            break;
+          }
+        }
+        st[2] += (unsigned long long)p.n_int;
+      }
+    }
+  }
+  warp_stats(d, st);
+}
+
+__global__ void __launch_bounds__(256) mc_persistent_kernel(McDev d) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
+  mc_photon p;
+  p.state = MC_DEAD;
+  p.n_int = 0;
+  bool retired = false;
+  unsigned long long pool_next = 0, pool_end = 0;  // warp-uniform
+  while (true) {
+    // ---- refill idle lanes with the next histories ----------------------
+    const unsigned need = __ballot_sync(FULL, p.state == MC_DEAD && !retired);
+    if (need) {
+      const unsigned cnt = __popc(need);
+      const unsigned rank = __popc(need & lt_mask);
+      const unsigned long long avail = pool_end - pool_next;
+      unsigned long long base = 0;
+      if (avail < cnt) {
+        if (lane == 0) base = atomicAdd(d.counter, (unsigned long long)kChunk);
+        base = __shfl_sync(FULL, base, 0);
+      }
+      if (need & (1u << lane)) {
+        unsigned long long h = rank < avail ? pool_next + rank : base + (rank - avail);
+        if (h >= d.total) {
+          retired = true;
+        } else {
+          int view, iu, iv;
+          unsigned long long k;
+          decompose(d, h, &view, &iu, &iv, &k);
+          st[2] += (unsigned long long)p.n_int;
+          mc_start(&d.P, d.T, d.V, d.U, d.W, view, iu, iv, k, &p);
+          st[0]++;
+        }
+      }
+      if (avail >= cnt) {
+        pool_next += cnt;
+      } else {
+        pool_next = base + (cnt - avail);
+        pool_end = base + kChunk;
+        if (pool_end > d.total) pool_end = d.total;
+        if (pool_next > pool_end) pool_next = pool_end;
+      }
+    }
+    if (__all_sync(FULL, retired)) break;
+    // ---- a few Woodcock steps ------------------------------------------
+#pragma unroll 1
+    for (int i = 0; i < kStepsPerRound && p.state == MC_FLY; i++) {
+      mc_flight_step(&d.P, d.T, d.labels, &p);
+      st[1]++;
+      if (p.state == MC_DEAD) st[5]++;
+    }
+    // ---- escaped photons: warp-aggregated tally --------------------------
+    long long key = -1;
+    long long cell = -1;
+    int kind = 0;
+    if (p.state == MC_ESCAPED) {
+      kind = mc_tally_kind(&d.P, &p);
+      cell = mc_detector_index(&d.P, d.V, &p);
+      if (kind >= 0 && cell >= 0) key = cell * 2 + kind;
+      p.state = MC_DEAD;
+    }
+    const unsigned tal = __ballot_sync(FULL, key >= 0);
+    if (key >= 0) {
+      const unsigned grp = __match_any_sync(tal, key);
+      if (lane == __ffs(grp) - 1) {
+        atomicAdd(kind == 0 ? &d.prim[cell] : &d.scat[cell], (unsigned long long)__popc(grp));
+      }
+      st[3 + kind]++;
+    }
+    // ---- real collisions, processed as a batch ---------------------------
+    const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
+    const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
+    if (coll && (__popc(coll) >= kCollideBatch || fly == 0)) {
+      if (p.state == MC_COLLIDED) p.state = mc_after_collision(&d.P, d.T, &p);
+    }
+  }
+  st[2] += (unsigned long long)p.n_int;
+  warp_stats(d, st);
+}
+
+__global__ void mc_finalize_kernel(size_t n, unsigned long long per, double log_per,
+                                   const long long* __restrict__ prim,
+                                   const long long* __restrict__ scat, int* __restrict__ proj0,
+                                   float* __restrict__ map0, int* __restrict__ proj5,
+                                   float* __restrict__ map5) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  long long a = prim ? prim[i] : 0;
+  long long b = a + (scat ? scat[i] : 0);
+  long long cap = (long long)per;
+  if (a > cap) a = cap;
+  if (a == 0) a = 1;
+  if (b > cap) b = cap;
+  if (b == 0) b = 1;
+  if (proj0) proj0[i] = (int)a;
+  if (map0) map0[i] = (float)(-log((double)a) + log_per);
+  if (proj5) proj5[i] = (int)b;
+  if (map5) map5[i] = (float)(-log((double)b) + log_per);
+}
+
+}  // namespace
+
+cudaError_t launch_mc(const McDev& d, int kernel, int sm_count, cudaStream_t st) {
+  if (kernel == 0) {
+    const int n = (d.P.u_end - d.P.u_begin) * (d.P.v_end - d.P.v_begin);
+    if (n == 0) return cudaSuccess;
+    mc_plain_kernel<<<(n + 127) / 128, 128, 0, st>>>(d);
+  } else {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_persistent_kernel,
+                                                                  256, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    mc_persistent_kernel<<<sm_count * per_sm, 256, 0, st>>>(d);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mc_finalize(size_t n, unsigned long long per, double log_per,
+                               const long long* prim, const long long* scat, int* proj0,
+                               float* map0, int* proj5, float* map5, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  mc_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, per, log_per, prim, scat,
+                                                                   proj0, map0, proj5, map5);
+  return cudaGetLastError();
+}
+
+}  // namespace monte

@@ -37,7 +37,7 @@ struct monte_ctx {
   monte::DevBuf scratch[16];
   // cached FDK device tables for the last geometry seen
   std::vector<uint8_t> fdk_key;
-  monte::DevBuf fdk_views, fdk_weights, fdk_taps, fdk_bsplit;
+  monte::DevBuf fdk_views, fdk_viewsd, fdk_weights, fdk_taps, fdk_bsplit;
   // cached MC device tables
   std::vector<uint8_t> mc_key;
   monte::DevBuf mc_tables, mc_views, mc_pixels;
@@ -46,6 +46,7 @@ struct monte_ctx {
   // autotuned backprojection tile choice, keyed by geometry
   std::vector<uint8_t> bp_tune_key;
   int bp_tune_choice = -1;
+  int last_bp_variant = -1;  // tile variant of the last backprojection, -1: plain kernel
 };
 
 namespace monte {

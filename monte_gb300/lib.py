@@ -45,6 +45,7 @@ def load(build_if_missing=False):
     lib.monte_last_error.restype = C.c_char_p
     lib.monte_ctx_set_stream.argtypes = [P, P]
     lib.monte_ctx_synchronize.argtypes = [P]
+    lib.monte_ctx_use_own_stream.argtypes = [P]
     lib.monte_fdk_geom_reference65.argtypes = [G]
     lib.monte_fdk_geom_reference65.restype = None
     lib.monte_fdk_geom_reference325.argtypes = [G]
@@ -52,6 +53,20 @@ def load(build_if_missing=False):
     lib.monte_fdk_filter.argtypes = [P, G, P, P, C.c_int, C.c_int]
     lib.monte_fdk_backproject.argtypes = [P, G, P, P, P, C.c_int, C.c_int]
     lib.monte_fdk.argtypes = [P, G, P, P, P, P, C.c_int, C.c_int, C.c_int]
+    lib.monte_fdk_autotune.argtypes = [P, G, C.POINTER(C.c_int)]
+    lib.monte_fdk_last_bp_variant.argtypes = [P]
+    lib.monte_ctx_check_status.argtypes = [P]
+    MG = C.POINTER(abi.McGeom)
+    lib.monte_mc_geom_reference325.argtypes = [MG]
+    lib.monte_mc_geom_reference325.restype = None
+    lib.monte_mc_geom_reference_cpu.argtypes = [MG]
+    lib.monte_mc_geom_reference_cpu.restype = None
+    lib.monte_xcom_parse_csv.argtypes = [C.c_char_p, C.c_size_t] + [C.POINTER(C.c_float)] * 4
+    lib.monte_mc_run.argtypes = [P, MG, C.POINTER(abi.McPhantom), C.POINTER(abi.McXcom),
+                                 C.POINTER(abi.McSpectrum), C.POINTER(abi.McRequest), P, P,
+                                 C.POINTER(abi.McStats), C.c_int]
+    lib.monte_mc_finalize.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P, P, P,
+                                      P, P, P, C.c_int]
     _LIB = lib
     return lib
 
@@ -73,6 +88,23 @@ def _mem_of(*arrays):
     if len(mems) != 1:
         raise ValueError("all arrays of one call must live in the same memory space")
     return mems.pop()
+
+
+def parse_xcom_csv(path_or_bytes):
+    """monte_xcom_parse_csv: an XCOM CSV -> float32 [4][201] (coh, incoh,
+    photo, total) indexed by keV.  Needs no GPU."""
+    lib = load()
+    if isinstance(path_or_bytes, (bytes, bytearray)):
+        data = bytes(path_or_bytes)
+    else:
+        with open(path_or_bytes, "rb") as f:
+            data = f.read()
+    out = np.zeros((4, 201), np.float32)
+    fp = C.POINTER(C.c_float)
+    rc = lib.monte_xcom_parse_csv(data, len(data), *[out[i].ctypes.data_as(fp) for i in range(4)])
+    if rc != 0:
+        raise MonteError(rc, "could not parse XCOM csv")
+    return out
 
 
 class Context:
@@ -118,6 +150,18 @@ class Context:
     def synchronize(self):
         self.check(self.lib.monte_ctx_synchronize(self.h))
 
+    def check_status(self):
+        """Raise MonteError(MONTE_ETIMEOUT) if a bounded device wait gave up."""
+        self.check(self.lib.monte_ctx_check_status(self.h))
+
+    def fdk_autotune(self, g):
+        best = C.c_int(-1)
+        self.check(self.lib.monte_fdk_autotune(self.h, C.byref(g), C.byref(best)))
+        return best.value
+
+    def last_bp_variant(self):
+        return self.lib.monte_fdk_last_bp_variant(self.h)
+
     # ---- FDK ----------------------------------------------------------
     def fdk_filter(self, g, proj, filtered, mode=abi.MONTE_FILTER_FP32):
         mem = _mem_of(proj, filtered)
@@ -128,6 +172,25 @@ class Context:
         mem = _mem_of(filtered, vol_xy, vol_zy)
         self.check(self.lib.monte_fdk_backproject(self.h, C.byref(g), _ptr(filtered)[0],
                                                   _ptr(vol_xy)[0], _ptr(vol_zy)[0], mode, mem))
+
+    # ---- Monte Carlo ----------------------------------------------------
+    def mc_run(self, g, inputs, request, primary, scatter):
+        """Add the histories of `request` into the int64 tallies; returns the
+        run statistics as a dict."""
+        mem = _mem_of(inputs.labels, primary, scatter)
+        st = abi.McStats()
+        self.check(self.lib.monte_mc_run(self.h, C.byref(g), C.byref(inputs.phantom),
+                                         C.byref(inputs.xcom), C.byref(inputs.spectrum),
+                                         C.byref(request), _ptr(primary)[0], _ptr(scatter)[0],
+                                         C.byref(st), mem))
+        return st.as_dict()
+
+    def mc_finalize(self, n_views, nu, nv, per, primary, scatter=None, proj0=None, map0=None,
+                    proj5=None, map5=None):
+        mem = _mem_of(primary, scatter, proj0, map0, proj5, map5)
+        self.check(self.lib.monte_mc_finalize(self.h, n_views, nu, nv, per, _ptr(primary)[0],
+                                              _ptr(scatter)[0], _ptr(proj0)[0], _ptr(map0)[0],
+                                              _ptr(proj5)[0], _ptr(map5)[0], mem))
 
     def fdk(self, g, proj, vol_xy, filtered=None, vol_zy=None,
             filter_mode=abi.MONTE_FILTER_FP32, bp_mode=abi.MONTE_BP_PLAIN):

@@ -90,6 +90,81 @@ def ellipsoid_line_integrals(g, ellipsoids, noise_sigma=0.0, seed=0, device="cpu
     return out.to(torch.float32)
 
 
+def sphere_labels_185():
+    """The label volume monte_cpp/make_image01.cpp:15-30 writes (spher01.raw):
+    185 x 185 x 325 voxels, label 1 inside the sphere of radius 50 voxels
+    centred on voxel (90, 90, 160), 0 elsewhere; layout [z][y][x].  With the
+    CPU program's lookup (monte_cpp/CBCT_real2.cpp:771) voxel (ix,iy,iz) covers
+    x in [(ix-90.5)/10, (ix-89.5)/10) cm, y likewise, z around (iz-160)/10."""
+    k, j, i = np.ogrid[0:325, 0:185, 0:185]
+    inside = (i - 90) ** 2 + (j - 90) ** 2 + (k - 160) ** 2 <= 2500
+    return inside.astype(np.uint8)
+
+
+# voxel size and low corner (cm) of sphere_labels_185() under CBCT_real2's lookup
+SPHERE185_VOXEL = 0.1
+SPHERE185_ORIGIN = (-9.05, -9.05, -16.05)
+
+
+def cylinder_inserts_labels(seed=1001, n=65, voxel_mm=1.0, radius_mm=28.0, insert_mm=5.0,
+                            place_mm=18.0):
+    """The 65^3 phantom of the CPU-runnable workload: water cylinder of radius
+    28 mm along z (label 1), three Ca-water inserts of radius 5 mm (labels 2,
+    3, 4 for densities 1.2 / 1.5 / 1.9) centred at seeded uniform positions
+    within 18 mm of the axis, not overlapping; air (label 0) outside.
+    Returns (labels[z][y][x] uint8, voxel cm, origin cm)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    centres = []
+    while len(centres) < 3:
+        r = place_mm * np.sqrt(rng.random())
+        a = 2 * np.pi * rng.random()
+        c = (r * np.cos(a), r * np.sin(a))
+        if all((c[0] - d[0]) ** 2 + (c[1] - d[1]) ** 2 > (2 * insert_mm + 1) ** 2 for d in centres):
+            centres.append(c)
+    ax = (np.arange(n) + 0.5 - n / 2.0) * voxel_mm
+    Z, Y, X = np.meshgrid(ax, ax, ax, indexing="ij")
+    lab = np.zeros((n, n, n), np.uint8)
+    lab[X * X + Y * Y <= radius_mm ** 2] = 1
+    for i, (cx, cy) in enumerate(centres):
+        lab[(X - cx) ** 2 + (Y - cy) ** 2 <= insert_mm ** 2] = 2 + i
+    h = n * voxel_mm / 2.0 / 10.0
+    return lab, voxel_mm / 10.0, (-h, -h, -h)
+
+
+def ellipsoid_labels(seed=1003, n=325, voxel_mm=0.8, n_ell=20):
+    """The 325^3 phantom of the full Monte Carlo workload: 20 seeded
+    ellipsoids (centres U(-80,80) mm, semi-axes U(10,70) mm, random
+    rotation) painted in order -- the first four are water (label 1), the
+    rest bone (Ca-water) with densities U(1.5, 1.9) g/cm^3, one label each --
+    air elsewhere.  Returns (labels uint8, voxel cm, origin cm, densities of
+    labels 0..n_labels-1, material of each label)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ax = ((np.arange(n) + 0.5 - n / 2.0) * voxel_mm / 10.0).astype(np.float32)
+    lab = np.zeros((n, n, n), np.uint8)
+    dens = [0.0, 1.0]
+    mats = [-1, 0]
+    for e in range(n_ell):
+        c = rng.uniform(-8.0, 8.0, 3)
+        a = rng.uniform(1.0, 7.0, 3)
+        R = _rotation(rng)
+        if e < 4:
+            label = 1
+        else:
+            dens.append(float(rng.uniform(1.5, 1.9)))
+            mats.append(1)
+            label = len(dens) - 1
+        for z in range(n):
+            Y, X = np.meshgrid(ax, ax, indexing="ij")
+            p = (X - c[0], Y - c[1], ax[z] - c[2])
+            r2 = 0.0
+            for i in range(3):
+                q = (R[0, i] * p[0] + R[1, i] * p[1] + R[2, i] * p[2]) / a[i]
+                r2 = r2 + q * q
+            lab[z][r2 <= 1.0] = label
+    h = n * voxel_mm / 2.0 / 10.0
+    return lab, voxel_mm / 10.0, (-h, -h, -h), dens, mats
+
+
 def ellipsoid_density(ellipsoids, X, Y, Z):
     """Sum of mu over ellipsoids containing the points (numpy/torch arrays)."""
     out = 0.0 * X

@@ -38,7 +38,70 @@ def lib():
         _LIB.oracle_fdk_filter_f64.argtypes = [g, f, d]
         _LIB.oracle_fdk_backproject.argtypes = [g, f, f, f, C.c_int, C.c_int]
         _LIB.oracle_fdk_backproject_f64.argtypes = [g, d, d, C.c_int, C.c_int]
+        from monte_gb300 import abi
+        _LIB.oracle_mc_run.argtypes = [C.POINTER(abi.McGeom), C.POINTER(abi.McPhantom),
+                                       C.POINTER(abi.McXcom), C.POINTER(abi.McSpectrum),
+                                       C.POINTER(abi.McRequest), C.c_void_p, C.c_void_p,
+                                       C.POINTER(C.c_uint64)]
+        _LIB.oracle_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_int, f]
+        u32 = C.POINTER(C.c_uint32)
+        _LIB.oracle_philox.argtypes = [u32, C.c_uint32, C.c_uint32, u32]
+        _LIB.oracle_logf.argtypes = [f, f, C.c_int]
+        _LIB.oracle_sincos_2pi.argtypes = [f, f, f, C.c_int]
+        _LIB.oracle_compton.argtypes = [C.c_float, C.c_uint64, C.c_int, f, f]
     return _LIB
+
+
+def mc_run(g, inputs, request):
+    """Replay of monte_mc_run on the CPU: (primary, scatter, stats) for a
+    request, tallies int64 [n_views][nu][nv] (labels must be host numpy)."""
+    prim = np.zeros((g.n_views, g.nu, g.nv), np.int64)
+    scat = np.zeros_like(prim)
+    st = (C.c_uint64 * 6)()
+    rc = lib().oracle_mc_run(C.byref(g), C.byref(inputs.phantom), C.byref(inputs.xcom),
+                             C.byref(inputs.spectrum), C.byref(request), prim.ctypes.data,
+                             scat.ctypes.data, st)
+    if rc != 0:
+        raise ValueError("oracle_mc_run rejected the inputs (%d)" % rc)
+    names = ("histories", "woodcock_steps", "interactions", "primary_counts",
+             "scatter_counts", "dropped")
+    return prim, scat, dict(zip(names, [int(x) for x in st]))
+
+
+def stream(seed, history, job, n):
+    out = np.zeros(n, np.float32)
+    lib().oracle_stream(seed, history, job, n, _fp(out))
+    return out
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, np.uint32)
+    out = np.zeros(4, np.uint32)
+    u32 = C.POINTER(C.c_uint32)
+    lib().oracle_philox(c.ctypes.data_as(u32), int(key[0]), int(key[1]), out.ctypes.data_as(u32))
+    return out
+
+
+def logf(x):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.zeros_like(x)
+    lib().oracle_logf(_fp(x), _fp(y), len(x))
+    return y
+
+
+def sincos_2pi(u):
+    u = np.ascontiguousarray(u, np.float32)
+    s, c = np.zeros_like(u), np.zeros_like(u)
+    lib().oracle_sincos_2pi(_fp(u), _fp(s), _fp(c), len(u))
+    return s, c
+
+
+def compton(E, seed, n):
+    """cos(theta) and scattered energy of n Compton events at E keV."""
+    ct = np.zeros(n, np.float32)
+    e = np.zeros(n, np.float32)
+    lib().oracle_compton(E, seed, n, _fp(ct), _fp(e))
+    return ct, e
 
 
 def _fp(a):

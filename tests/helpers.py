@@ -48,3 +48,24 @@ def past_end_voxels(g):
     mask = np.zeros((g.nz, g.ny, g.nx), bool)
     mask[:, :, g.s_begin:g.s_end] = hit
     return mask
+
+
+def chi2_two_sample(a, b, na=1.0, nb=1.0, min_count=20):
+    """Two-sample chi-square for Poisson counts a (exposure na) and b
+    (exposure nb) over bins with a + b >= min_count:
+    sum (a*sqrt(nb/na) - b*sqrt(na/nb))^2 / (a + b).  Returns (chi2, dof,
+    p-value)."""
+    from scipy.stats import chi2 as _chi2
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    m = (a + b) >= min_count
+    k1, k2 = np.sqrt(nb / na), np.sqrt(na / nb)
+    x2 = float(np.sum((k1 * a[m] - k2 * b[m]) ** 2 / (a[m] + b[m])))
+    dof = int(m.sum())
+    return x2, dof, float(_chi2.sf(x2, dof))
+
+
+def block_sum(img, k):
+    """Sum k x k blocks of a 2-D image (cropped to a multiple of k)."""
+    h, w = (img.shape[0] // k) * k, (img.shape[1] // k) * k
+    return img[:h, :w].reshape(h // k, k, w // k, k).sum(axis=(1, 3))

@@ -1,0 +1,143 @@
+"""Monte Carlo on the GPU through the C ABI.
+
+* Seeded replay: the plain and the persistent kernels produce int64 tallies
+  bit-equal to the CPU replay harness (same Philox streams, same step
+  functions), for monochromatic and polychromatic sources and every physics
+  switch.
+* Physics: chi-square against the reference CPU program's 10^7-history
+  scatter image (tests/golden/cbct_real2.npz).
+* Post-processing equals the reference formula (CBCT_real325im.cu:261-294).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from helpers import block_sum, chi2_two_sample, golden
+from monte_gb300 import abi, phantoms
+
+pytestmark = pytest.mark.gpu
+
+
+def cfg1_inputs(device=None, spectrum="mono"):
+    x = golden("xcom")
+    lab, vox, org = phantoms.cylinder_inserts_labels()
+    if device is not None:
+        lab = torch.from_numpy(lab).to(device)
+    if spectrum == "mono":
+        E, W = [60.0], None
+    else:
+        E = np.arange(20.0, 81.0)
+        W = 80.0 - E
+    return abi.McInputs(lab, vox, org, [-1, 0, 1, 1, 1], [0.0, 1.0, 1.2, 1.5, 1.9],
+                        [x["water"], x["ca"]], E, W)
+
+
+def cfg1_geom(flags=abi.MONTE_MC_STALE_SIN_PHI):
+    # 64x64 pixels of 1 mm, SOD 500 mm, SDD 1000 mm, 90 views
+    return abi.mc_geom(90, 64, 64, 0.1, 50.0, 100.0, 3.5, flags=flags)
+
+
+def _gpu_run(ctx, g, inp_dev, req):
+    prim = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device="cuda")
+    scat = torch.zeros_like(prim)
+    st = ctx.mc_run(g, inp_dev, req, prim, scat)
+    ctx.synchronize()
+    return prim.cpu().numpy(), scat.cpu().numpy(), st
+
+
+@pytest.mark.parametrize("spectrum", ["mono", "poly"])
+@pytest.mark.parametrize("flags", [abi.MONTE_MC_STALE_SIN_PHI, 0,
+                                   abi.MONTE_MC_FIRST_COMPTON_Z | abi.MONTE_MC_NO_RAYLEIGH_TALLY])
+def test_replay_is_bit_exact(ctx, spectrum, flags):
+    g = cfg1_geom(flags)
+    host = cfg1_inputs(None, spectrum)
+    dev = cfg1_inputs("cuda", spectrum)
+    req = abi.mc_request(31337, 6, (10, 13), (0, 64), (0, 64))
+    p_ref, s_ref, st_ref = oracle.mc_run(g, host, req)
+    assert s_ref.sum() > 0 and p_ref.sum() > 0
+    for kernel in (abi.MONTE_MC_PLAIN, abi.MONTE_MC_PERSISTENT):
+        req.kernel = kernel
+        p, s, st = _gpu_run(ctx, g, dev, req)
+        assert np.array_equal(p, p_ref), kernel
+        assert np.array_equal(s, s_ref), kernel
+        assert st["histories"] == st_ref["histories"]
+        assert st["woodcock_steps"] == st_ref["woodcock_steps"]
+        assert st["interactions"] == st_ref["interactions"]
+
+
+def test_split_runs_sum_to_the_whole(ctx):
+    """Any partition of (views, pixels) reproduces the single run's tallies:
+    the sharding contract for multi-GPU runs."""
+    g = cfg1_geom()
+    dev = cfg1_inputs("cuda")
+    whole = _gpu_run(ctx, g, dev, abi.mc_request(9, 5, (0, 4), (0, 64), (0, 64)))
+    prim = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device="cuda")
+    scat = torch.zeros_like(prim)
+    for views in ((0, 1), (1, 4)):
+        for us in ((0, 20), (20, 64)):
+            ctx.mc_run(g, dev, abi.mc_request(9, 5, views, us, (0, 64)), prim, scat)
+    ctx.synchronize()
+    assert np.array_equal(prim.cpu().numpy(), whole[0])
+    assert np.array_equal(scat.cpu().numpy(), whole[1])
+
+
+@pytest.mark.parametrize("kernel", [abi.MONTE_MC_PLAIN, abi.MONTE_MC_PERSISTENT])
+def test_scatter_image_matches_cbct_real2(ctx, kernel):
+    gold = golden("cbct_real2")
+    n = int(gold["histories"])
+    x = golden("xcom")
+    lab = torch.from_numpy(phantoms.sphere_labels_185()).cuda()
+    inp = abi.McInputs(lab, phantoms.SPHERE185_VOXEL, phantoms.SPHERE185_ORIGIN, [-1, 0],
+                       [0.0, 1.0], [x["water"]], [140.0])
+    g = abi.mc_geom_reference_cpu()
+    p, s, st = _gpu_run(ctx, g, inp, abi.mc_request(77, n, (0, 1), (32, 33), (32, 33), kernel))
+    assert st["histories"] == n and st["dropped"] == 0
+    for k in (1, 5):
+        x2, dof, pv = chi2_two_sample(block_sum(s[0], k), block_sum(gold["image"], k), n, n)
+        assert pv > 1e-3, (k, x2, dof, pv)
+
+
+def test_finalize_matches_reference_formula(ctx):
+    rng = np.random.default_rng(3)
+    per = 2000
+    prim = rng.integers(0, 2500, size=(4, 8, 8)).astype(np.int64)
+    prim[0, 0, :3] = 0
+    scat = rng.integers(0, 300, size=(4, 8, 8)).astype(np.int64)
+    outs = [np.zeros((4, 8, 8), np.int32), np.zeros((4, 8, 8), np.float32),
+            np.zeros((4, 8, 8), np.int32), np.zeros((4, 8, 8), np.float32)]
+    ctx.mc_finalize(4, 8, 8, per, prim, scat, *outs)
+    for tally, proj, mp in ((prim, outs[0], outs[1]), (prim + scat, outs[2], outs[3])):
+        n = np.clip(tally, None, per)
+        n[n == 0] = 1
+        assert np.array_equal(proj, n.astype(np.int32))
+        want = (-np.log(n.astype(np.float64)) + np.float64(np.float32(np.log(per)))).astype(np.float32)
+        assert np.array_equal(mp, want)
+
+
+def test_host_memory_path(ctx):
+    g = cfg1_geom()
+    req = abi.mc_request(4, 3, (0, 2), (0, 64), (0, 64))
+    d = _gpu_run(ctx, g, cfg1_inputs("cuda"), req)
+    host = cfg1_inputs(None)
+    prim = np.zeros((g.n_views, g.nu, g.nv), np.int64)
+    scat = np.zeros_like(prim)
+    ctx.mc_run(g, host, req, prim, scat)
+    assert np.array_equal(prim, d[0]) and np.array_equal(scat, d[1])
+
+
+def test_bad_arguments(ctx):
+    from monte_gb300.lib import MonteError
+    g = cfg1_geom()
+    dev = cfg1_inputs("cuda")
+    prim = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device="cuda")
+    for bad in (dict(view_end=91), dict(u_end=65), dict(kernel=5)):
+        req = abi.mc_request(1, 1, (0, 1), (0, 64), (0, 64))
+        for k, v in bad.items():
+            setattr(req, k, v)
+        with pytest.raises(MonteError) as e:
+            ctx.mc_run(g, dev, req, prim, prim.clone())
+        assert e.value.code == abi.MONTE_EINVAL
+    g.sdd = 10.0  # detector inside the source distance
+    with pytest.raises(MonteError):
+        ctx.mc_run(g, dev, abi.mc_request(1, 1, (0, 1), (0, 64), (0, 64)), prim, prim.clone())
