@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form FDK timing")
     ap.add_argument("--no-mc", action="store_true", help="skip the Monte Carlo timing")
+    ap.add_argument("--tile", type=int, default=-1,
+                    help="backprojection tile shape (default: autotune)")
     ap.add_argument("--small", action="store_true", help="reduced sizes (for profiling runs)")
     return ap.parse_args()
 
@@ -53,7 +55,9 @@ WORKLOAD = "fdk: 360 views x 512(u) x 384(v) FP32 @0.8mm, SOD 500, SDD 1000 mm -
 def geometry(small=False):
     from monte_gb300.abi import fdk_geom_recon325
     if small:
-        return fdk_geom_recon325(n_views=90, nu=512, nv=384, n=163, voxel_mm=0.8)
+        # profiling case: the same detector and volume over 180 views (141 MB of
+        # projections, above the 129 MB L2)
+        return fdk_geom_recon325(n_views=180)
     return fdk_geom_recon325()
 
 
@@ -275,7 +279,11 @@ def run_ours(args):
     bmode = abi.MONTE_BP_TILED if args.bp == "tiled" else abi.MONTE_BP_PLAIN
 
     proj = make_input(g, dev)
-    tile = ctx.fdk_autotune(g) if bmode == abi.MONTE_BP_TILED else -1
+    if args.tile >= 0:
+        tile = args.tile
+        ctx.set_bp_variant(tile)
+    else:
+        tile = ctx.fdk_autotune(g) if bmode == abi.MONTE_BP_TILED else -1
     filt = torch.empty((g.n_views, g.nv, g.nu), dtype=torch.float32, device=dev)
     vol = torch.empty((g.nz, g.ny, g.nx), dtype=torch.float32, device=dev)
     updates = g.nx * g.ny * g.nz * g.n_views

@@ -145,6 +145,20 @@ int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* 
 int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
               float* vol_xy, float* vol_zy, int filter_mode, int bp_mode, int mem);
 
+/* Exact adjoint of monte_fdk_backproject (MONTE_BP_PLAIN coefficients): the
+ * ray-driven cone-beam forward projector, vol_xy[nz][ny][nx] ->
+ * filtered_out[view][v][u] (overwritten).  Needs flags without
+ * MONTE_FDK_FLAT_EDGE (MONTE_EUNSUPPORTED otherwise).  No counterpart in
+ * the reference; the transpose of recon/bp3d20.cpp:81-166. */
+int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const float* vol_xy,
+                              float* filtered_out, int mem);
+/* Adjoint of the whole FDK (monte_fdk with MONTE_FILTER_FP32 and
+ * MONTE_BP_PLAIN): grad_proj[view][u][v] = W * T^T * A^T grad_vol, the
+ * gradient of <grad_vol, FDK(proj)> with respect to proj.  Same flag
+ * condition as monte_fdk_forward_project. */
+int monte_fdk_backward(monte_ctx* ctx, const monte_fdk_geom* g, const float* grad_vol,
+                       float* grad_proj, int mem);
+
 /* Backprojection autotuner (no counterpart in the reference, whose
  * backprojection is a fixed CPU loop nest, recon/bp3d20.cpp:83-166): times
  * every tile shape (voxels per thread along z, columns per CTA, views per
@@ -152,6 +166,10 @@ int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float*
  * the context's choice for MONTE_BP_TILED.  *best receives its index, or -1
  * if no tile shape fits g (MONTE_BP_TILED then runs the plain kernel). */
 int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best);
+/* Choose the tile shape MONTE_BP_TILED uses on this context (-1: the
+ * default shape); a shape that does not fit a geometry falls back to the
+ * default, then to the plain kernel. */
+int monte_fdk_set_bp_variant(monte_ctx* ctx, int variant);
 /* Which kernel the last monte_fdk_backproject/monte_fdk call of this context
  * ran: a tile shape index >= 0, or -1 for MONTE_BP_PLAIN. */
 int monte_fdk_last_bp_variant(const monte_ctx* ctx);
@@ -294,6 +312,36 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
 int monte_mc_finalize(monte_ctx* ctx, int32_t n_views, int32_t nu, int32_t nv, uint64_t per,
                       const int64_t* primary, const int64_t* scatter, int32_t* proj0,
                       float* map0, int32_t* proj5, float* map5, int mem);
+
+/* ======================================================================
+ *  Primary signal (differentiable mode)
+ * ====================================================================== */
+
+/* Voxel grid of an attenuation volume mu[nz][ny][nx] (1/cm), same
+ * conventions as monte_mc_phantom. */
+typedef struct monte_siddon_grid {
+  int32_t nx, ny, nz, reserved0;
+  double dx, dy, dz;
+  double x0, y0, z0;
+} monte_siddon_grid;
+
+/* Expected primary signal of the Monte Carlo: for every pixel (i, j) of the
+ * views [view_begin, view_end), the line integral L of mu along the
+ * emission ray the Monte Carlo aims at that pixel
+ * (monte_cu/CBCT_real325im.cu:476-512) by Siddon's exact voxel traversal,
+ * and the transmission exp(-L) -- the expectation of the primary tally per
+ * history (:567-590).  line / transmission are [n_views][nu][nv] (either may
+ * be NULL); only the requested views are written. */
+int monte_siddon_forward(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid,
+                         const float* mu, int view_begin, int view_end, float* line,
+                         float* transmission, int mem);
+/* Adjoint of monte_siddon_forward: grad_mu[v] += sum over rays of
+ * (grad_line + grad_transmission * d exp(-L)/dL) * (length of the ray in
+ * voxel v).  The line integrals are recomputed, not read back.  Either
+ * gradient may be NULL.  Accumulation order is not fixed (float atomics). */
+int monte_siddon_backward(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid,
+                          const float* mu, int view_begin, int view_end, const float* grad_line,
+                          const float* grad_transmission, float* grad_mu, int mem);
 
 #ifdef __cplusplus
 }

@@ -289,6 +289,23 @@ def mc_request(seed, per, views, u_range, v_range, kernel=MONTE_MC_PERSISTENT, j
     return r
 
 
+class SiddonGrid(C.Structure):
+    """monte_siddon_grid."""
+
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("reserved0", C.c_int32), ("dx", C.c_double), ("dy", C.c_double),
+                ("dz", C.c_double), ("x0", C.c_double), ("y0", C.c_double),
+                ("z0", C.c_double)]
+
+
+def siddon_grid(shape_zyx, voxel_cm, origin_cm):
+    g = SiddonGrid()
+    g.nz, g.ny, g.nx = shape_zyx
+    g.dx, g.dy, g.dz = voxel_cm if hasattr(voxel_cm, "__len__") else (voxel_cm,) * 3
+    g.x0, g.y0, g.z0 = origin_cm
+    return g
+
+
 def fdk_geom_recon325(n_views=360, nu=512, nv=384, pitch_mm=0.8, sod_mm=500.0,
                       sdd_mm=1000.0, n=325, voxel_mm=0.4):
     """FDK at the recon-325 workload: 360 views of a 512 (in-plane) x 384

@@ -65,6 +65,13 @@ cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const BpVi
 cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
                                 const float* filtered, float* vol_xy, float* vol_zy,
                                 int variant, int* status, cudaStream_t st);
+// Adjoints (fdk_adjoint.cu): forward projector = transpose of the plain
+// backprojector, into filtered-space layout [view][v][u]; adjoint of the
+// weighting + filter, [view][v][u] -> [view][u][v].
+cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
+                                       const float* vol, float* out, cudaStream_t st);
+cudaError_t launch_fdk_filter_adjoint(const FdkDev& d, const float* g, const float* weights,
+                                      const float* taps_half, float* h, cudaStream_t st);
 int fdk_bp_tiled_variants();
 bool fdk_bp_tiled_supported(const FdkDev& d, int variant);
 
@@ -150,6 +157,64 @@ __device__ __forceinline__ bool bp_near_edge(const FdkDev& d, float ts, float up
   return fabsf(ts) < 1e-4f || fabsf(fabsf(up) - d.half_u) < 1e-4f * d.half_u ||
          fabsf(fabsf(vp) - d.half_v) < 1e-4f * d.half_v || fabsf(x - d.xmax) < 1e-3f ||
          fabsf(y - d.ymax) < 1e-3f || fabsf(x) < 1e-3f || fabsf(y) < 1e-3f;
+}
+
+// Coefficients of one voxel-view pair of the backprojection operator:
+// vol[s,t,z] += w * factor * bilinear(F_k; xi + fx, yi + fy).  Returns false
+// when the pair contributes nothing (rejected by recon/bp3d20.cpp:116, or
+// outside the interpolation guard of :152).  The plain backprojector and
+// its adjoint (the forward projector) both use this function, so the two
+// are exact transposes of each other.
+__device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const BpViewD& vd, int s,
+                                        int t, int z, float X, float Y, float Z, int* xi, int* yi,
+                                        float* fx, float* fy, float* w) {
+  float ax = X - v.px, ay = Y - v.py;
+  float Vx = ax * v.c + ay * v.s;
+  float Vy = ay * v.c - ax * v.s;
+  float kk = d.sdd / Vx;
+  float up = Vy * kk, vp = Z * kk;
+  float y = (d.half_u - up) * d.inv_du;
+  float x = (d.half_v - vp) * d.inv_dv;
+  float ts = X * v.c - Y * v.s;
+  if (!bp_near_edge(d, ts, up, vp, x, y)) {
+    if (fabsf(up) > d.half_u || fabsf(vp) > d.half_v) return false;
+    if (!(x >= 0.f && x <= d.xmax && y >= 0.f && y <= d.ymax)) return false;
+    float tt = X * v.s + Y * v.c;
+    float dd = fabsf(ts - v.tanb * tt) * v.rs;
+    if (ts < 0.f) dd = -dd;
+    float den = d.D - dd;
+    *w = (d.D * d.D) / (den * den);
+    *xi = (int)x;
+    *yi = (int)y;
+    *fx = x - (float)*xi;
+    *fy = y - (float)*yi;
+    return true;
+  }
+  double xd, yd, wd;
+  if (!bp_ref_voxel(d, vd, s, t, z, &xd, &yd, &wd)) return false;
+  if (!(xd >= 0.0 && xd <= (double)d.nv && yd >= 0.0 && yd <= (double)d.nu)) return false;
+  *w = (float)wd;
+  *xi = (int)xd;
+  *yi = (int)yd;
+  *fx = (float)(xd - *xi);
+  *fy = (float)(yd - *yi);
+  return true;
+}
+
+// Bilinear read at integer corner (xi, yi) with fractions (fx, fy), with the
+// reference's flat-array edge semantics (see bp_bilinear_global).
+__device__ __forceinline__ float bp_bilinear_at(const FdkDev& d, const float* __restrict__ f, int k,
+                                                int xi, int yi, float fx, float fy) {
+  const size_t total = (size_t)d.n_views * d.nu * d.nv;
+  size_t i00 = (size_t)k * d.nu * d.nv + (size_t)xi * d.nu + yi;
+  bool flat = (d.flags & MONTE_FDK_FLAT_EDGE) != 0;
+  float f00 = bp_fetch(f, total, i00, flat || (xi < d.nv && yi < d.nu));
+  float f10 = bp_fetch(f, total, i00 + d.nu, flat || (xi + 1 < d.nv && yi < d.nu));
+  float f01 = bp_fetch(f, total, i00 + 1, flat || (xi < d.nv && yi + 1 < d.nu));
+  float f11 = bp_fetch(f, total, i00 + d.nu + 1, flat || (xi + 1 < d.nv && yi + 1 < d.nu));
+  float r0 = fmaf(fx, f10 - f00, f00);
+  float r1 = fmaf(fx, f11 - f01, f01);
+  return fmaf(fy, r1 - r0, r0);
 }
 
 #endif

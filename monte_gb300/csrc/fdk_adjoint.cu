@@ -1,0 +1,199 @@
+// fdk_adjoint.cu -- exact adjoints of the FDK operator for the
+// differentiable mode.
+//
+//  * Forward projector = transpose of the voxel-driven backprojection
+//    (recon/bp3d20.cpp:81-166): G[k][row][col] = sum over voxels of
+//    w * factor * (bilinear weight of (row, col)) * R[z][t][s], with the
+//    coefficients of bp_coef, the function the plain backprojector uses.
+//    Ray-driven: a CTA owns one view and a block of detector columns; it
+//    enumerates the voxel columns in the wedge of source rays that project
+//    onto its detector columns (for each voxel row along the view's major
+//    axis, the range along the other axis follows from the perspective
+//    map), walks each candidate column along z, and accumulates into a
+//    shared-memory copy of its detector columns before one coalesced store.
+//  * Adjoint of the weighting + ramp filter (recon/bp3d20.cpp:36-73): the
+//    Toeplitz matrix is symmetric, so the transpose filters along u again,
+//    reading [view][v][u] and writing [view][u][v], then applies the cosine
+//    weight.
+#include "fdk.cuh"
+
+namespace monte {
+namespace {
+
+constexpr int FP_COLS = 32;    // detector columns per CTA
+constexpr int FP_THREADS = 256;
+
+__global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* __restrict__ views,
+                                                        const BpViewD* __restrict__ viewsd,
+                                                        const float* __restrict__ vol,
+                                                        float* __restrict__ out) {
+  extern __shared__ float G[];  // [nv][FP_COLS]
+  const int k = blockIdx.y;
+  const int c0 = blockIdx.x * FP_COLS;
+  const int ncols = min(FP_COLS, d.nu - c0);
+  for (int i = threadIdx.x; i < d.nv * FP_COLS; i += FP_THREADS) G[i] = 0.f;
+  __syncthreads();
+  const BpView v = views[k];
+  const BpViewD vd = viewsd[k];
+  // u' range of the detector columns [c0 - 1, c0 + ncols] (one column of
+  // margin either side), as y = (half_u - u') / du
+  const float ua = d.half_u - (float)(c0 + ncols + 1) * (1.0f / d.inv_du);
+  const float ub = d.half_u - (float)(c0 - 2) * (1.0f / d.inv_du);
+  const bool x_major = fabsf(v.c) >= fabsf(v.s);
+  const int n_major = x_major ? (d.s_end - d.s_begin) : d.ny;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int m = warp; m < n_major; m += FP_THREADS / 32) {
+    // minor-axis range of the wedge on this voxel row
+    int lo, hi;
+    if (x_major) {
+      const int s = d.s_begin + m;
+      const float X = fmaf((float)s, d.dvox, d.x0);
+      const float ax = X - v.px;
+      float Ys[2];
+      for (int e = 0; e < 2; e++) {
+        float u = e ? ub : ua;
+        float den = u * v.s - d.sdd * v.c;
+        Ys[e] = v.py - ax * (u * v.c + d.sdd * v.s) / den;
+      }
+      float tA = (d.y0 - Ys[0]) / d.dvox, tB = (d.y0 - Ys[1]) / d.dvox;
+      lo = max((int)floorf(fminf(tA, tB)) - 2, 0);
+      hi = min((int)ceilf(fmaxf(tA, tB)) + 2, d.ny - 1);
+    } else {
+      const int t = m;
+      const float Y = fmaf(-(float)t, d.dvox, d.y0);
+      const float ay = Y - v.py;
+      float Xs[2];
+      for (int e = 0; e < 2; e++) {
+        float u = e ? ub : ua;
+        float den = u * v.c + d.sdd * v.s;
+        Xs[e] = v.px - ay * (u * v.s - d.sdd * v.c) / den;
+      }
+      float sA = (Xs[0] - d.x0) / d.dvox, sB = (Xs[1] - d.x0) / d.dvox;
+      lo = max((int)floorf(fminf(sA, sB)) - 2, d.s_begin);
+      hi = min((int)ceilf(fmaxf(sA, sB)) + 2, d.s_end - 1);
+    }
+    for (int q = lo + lane; q <= hi; q += 32) {
+      const int s = x_major ? d.s_begin + m : q;
+      const int t = x_major ? q : m;
+      const float X = fmaf((float)s, d.dvox, d.x0);
+      const float Y = fmaf(-(float)t, d.dvox, d.y0);
+      // cheap column test: does this voxel column project near our columns?
+      {
+        float ax = X - v.px, ay = Y - v.py;
+        float Vx = ax * v.c + ay * v.s;
+        float Vy = ay * v.c - ax * v.s;
+        float y = (d.half_u - Vy * (d.sdd / Vx)) * d.inv_du;
+        if (!(y >= (float)(c0 - 2) && y < (float)(c0 + ncols + 1))) continue;
+      }
+      for (int z = 0; z < d.nz; z++) {
+        if (d.mask_r2 > 0) {
+          int a = z - d.cz, b = t - d.ct, c = s - d.cs;
+          if (a * a + b * b + c * c > d.mask_r2) continue;
+        }
+        const float Z = fmaf(-(float)z, d.dvox, d.z0);
+        int xi, yi;
+        float fx, fy, w;
+        if (!bp_coef(d, v, vd, s, t, z, X, Y, Z, &xi, &yi, &fx, &fy, &w)) continue;
+        const float r = __ldg(vol + ((size_t)z * d.ny + t) * d.nx + s);
+        if (r == 0.f) continue;
+        const float c = w * r * v.factor;
+#pragma unroll
+        for (int dy = 0; dy < 2; dy++) {
+          const int col = yi + dy - c0;
+          if (col < 0 || col >= ncols || yi + dy >= d.nu) continue;
+          const float wy = dy ? fy : 1.f - fy;
+#pragma unroll
+          for (int dx = 0; dx < 2; dx++) {
+            const int row = xi + dx;
+            if (row >= d.nv) continue;
+            const float wx = dx ? fx : 1.f - fx;
+            atomicAdd(&G[row * FP_COLS + col], c * wx * wy);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  float* dst = out + (size_t)k * d.nu * d.nv;
+  for (int i = threadIdx.x; i < d.nv * FP_COLS; i += FP_THREADS) {
+    int row = i / FP_COLS, col = i % FP_COLS;
+    if (col < ncols) dst[(size_t)row * d.nu + c0 + col] = G[i];
+  }
+}
+
+// H[n][c][v] = w[c][v] * sum_b T[b][c] * G[n][v][b]  (T symmetric)
+constexpr int TM = 64, TN = 64, TK = 16;
+__global__ void __launch_bounds__(256) filter_adjoint_kernel(int nu, int nv,
+                                                             const float* __restrict__ g,
+                                                             const float* __restrict__ weights,
+                                                             const float* __restrict__ taps_half,
+                                                             float* __restrict__ h) {
+  __shared__ __align__(16) float As[TK][TM];  // [b][v]
+  __shared__ __align__(16) float Bs[TK][TN];  // [b][c]
+  const int n = blockIdx.z;
+  const int v0 = blockIdx.y * TM;
+  const int c0 = blockIdx.x * TN;
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const float* G = g + (size_t)n * nu * nv;
+  float acc[4][4] = {};
+  for (int b0 = 0; b0 < nu; b0 += TK) {
+#pragma unroll
+    for (int i = 0; i < (TK * TM) / 256; i++) {
+      int e = tid + i * 256;
+      int r = e % TK, col = e / TK;  // r: b offset (fastest in memory), col: v
+      int b = b0 + r, v = v0 + col;
+      As[r][col] = (b < nu && v < nv) ? G[(size_t)v * nu + b] : 0.f;
+      int e2 = tid + i * 256;
+      int r2 = e2 / TN, cc = e2 % TN;
+      int bb = b0 + r2, c = c0 + cc;
+      Bs[r2][cc] = (bb < nu && c < nu) ? taps_half[bb - c + nu - 1] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; kk++) {
+      float4 a4 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+      float4 b4 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      float a[4] = {a4.x, a4.y, a4.z, a4.w};
+      float bb[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  float* H = h + (size_t)n * nu * nv;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    int c = c0 + tx * 4 + j;
+    if (c >= nu) continue;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      int v = v0 + ty * 4 + i;
+      if (v < nv) H[(size_t)c * nv + v] = acc[i][j] * weights[(size_t)c * nv + v];
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
+                                       const float* vol, float* out, cudaStream_t st) {
+  size_t smem = (size_t)d.nv * FP_COLS * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(fp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((d.nu + FP_COLS - 1) / FP_COLS, d.n_views);
+  fp_kernel<<<grid, FP_THREADS, smem, st>>>(d, views, viewsd, vol, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fdk_filter_adjoint(const FdkDev& d, const float* g, const float* weights,
+                                      const float* taps_half, float* h, cudaStream_t st) {
+  dim3 grid((d.nu + TN - 1) / TN, (d.nv + TM - 1) / TM, d.n_views);
+  filter_adjoint_kernel<<<grid, 256, 0, st>>>(d.nu, d.nv, g, weights, taps_half, h);
+  return cudaGetLastError();
+}
+
+}  // namespace monte

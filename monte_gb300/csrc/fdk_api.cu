@@ -404,4 +404,88 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
 
 int monte_fdk_last_bp_variant(const monte_ctx* ctx) { return ctx ? ctx->last_bp_variant : -1; }
 
+int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const float* vol_xy,
+                              float* filtered_out, int mem) {
+  if (!ctx) return MONTE_EINVAL;
+  MONTE_TRY(validate(ctx, g, true));
+  if (!vol_xy || !filtered_out) return set_error(ctx, MONTE_EINVAL, "null volume/output pointer");
+  if (g->flags & MONTE_FDK_FLAT_EDGE)
+    return set_error(ctx, MONTE_EUNSUPPORTED,
+                     "the adjoint is defined for the operator without MONTE_FDK_FLAT_EDGE");
+  if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
+    return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(prepare_tables(ctx, g));
+  FdkDev d = make_fdk_dev(*g);
+  const size_t pb = proj_bytes(g), vb = vol_bytes(g);
+  const float* dv = vol_xy;
+  float* dout = filtered_out;
+  if (mem == MONTE_MEM_HOST) {
+    MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "volume staging"));
+    MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "projection staging"));
+    MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->scratch[kScratchVolXY].ptr, vol_xy, vb,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    dv = (const float*)ctx->scratch[kScratchVolXY].ptr;
+    dout = (float*)ctx->scratch[kScratchFiltered].ptr;
+  }
+  cudaError_t e = launch_fdk_forward_project(d, (const BpView*)ctx->fdk_views.ptr,
+                                             (const BpViewD*)ctx->fdk_viewsd.ptr, dv, dout,
+                                             ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "forward projection launch");
+  if (mem == MONTE_MEM_HOST) {
+    MONTE_CUDA(ctx, cudaMemcpyAsync(filtered_out, dout, pb, cudaMemcpyDeviceToHost, ctx->stream));
+    MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return MONTE_OK;
+}
+
+int monte_fdk_backward(monte_ctx* ctx, const monte_fdk_geom* g, const float* grad_vol,
+                       float* grad_proj, int mem) {
+  if (!ctx) return MONTE_EINVAL;
+  MONTE_TRY(validate(ctx, g, true));
+  if (!grad_vol || !grad_proj) return set_error(ctx, MONTE_EINVAL, "null gradient pointer");
+  if (g->flags & MONTE_FDK_FLAT_EDGE)
+    return set_error(ctx, MONTE_EUNSUPPORTED,
+                     "the adjoint is defined for the operator without MONTE_FDK_FLAT_EDGE");
+  if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
+    return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(prepare_tables(ctx, g));
+  FdkDev d = make_fdk_dev(*g);
+  const size_t pb = proj_bytes(g), vb = vol_bytes(g);
+  MONTE_TRY(ensure_slot(ctx, kScratchAux0, pb, "adjoint scratch"));
+  float* tmp = (float*)ctx->scratch[kScratchAux0].ptr;
+  const float* dv = grad_vol;
+  float* dout = grad_proj;
+  if (mem == MONTE_MEM_HOST) {
+    MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "volume staging"));
+    MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
+    MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->scratch[kScratchVolXY].ptr, grad_vol, vb,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    dv = (const float*)ctx->scratch[kScratchVolXY].ptr;
+    dout = (float*)ctx->scratch[kScratchProj].ptr;
+  }
+  cudaError_t e = launch_fdk_forward_project(d, (const BpView*)ctx->fdk_views.ptr,
+                                             (const BpViewD*)ctx->fdk_viewsd.ptr, dv, tmp,
+                                             ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_fdk_filter_adjoint(d, tmp, (const float*)ctx->fdk_weights.ptr,
+                                  (const float*)ctx->fdk_taps.ptr, dout, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "FDK backward launch");
+  if (mem == MONTE_MEM_HOST) {
+    MONTE_CUDA(ctx, cudaMemcpyAsync(grad_proj, dout, pb, cudaMemcpyDeviceToHost, ctx->stream));
+    MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return MONTE_OK;
+}
+
+int monte_fdk_set_bp_variant(monte_ctx* ctx, int variant) {
+  if (!ctx) return MONTE_EINVAL;
+  if (variant < -1 || variant >= fdk_bp_tiled_variants())
+    return set_error(ctx, MONTE_EINVAL, "tile shape %d out of range [-1,%d)", variant,
+                     fdk_bp_tiled_variants());
+  ctx->bp_tune_choice = variant;
+  return MONTE_OK;
+}
+
 }  // extern "C"

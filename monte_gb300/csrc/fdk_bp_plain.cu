@@ -37,31 +37,10 @@ __global__ void __launch_bounds__(256) bp_plain_kernel(FdkDev d, const BpView* _
     const float Z = fmaf(-(float)z, d.dvox, d.z0);
     for (int k = 0; k < d.n_views; k++) {
       const BpView v = views[k];
-      float ax = X - v.px, ay = Y - v.py;
-      float Vx = ax * v.c + ay * v.s;
-      float Vy = ay * v.c - ax * v.s;
-      float kk = d.sdd / Vx;
-      float up = Vy * kk, vp = Z * kk;
-      float y = (d.half_u - up) * d.inv_du;
-      float x = (d.half_v - vp) * d.inv_dv;
-      float ts = X * v.c - Y * v.s;
-      float w, val = 0.f;
-      if (!bp_near_edge(d, ts, up, vp, x, y)) {
-        if (fabsf(up) > d.half_u || fabsf(vp) > d.half_v) continue;  // recon/bp3d20.cpp:116
-        if (x >= 0.f && x <= d.xmax && y >= 0.f && y <= d.ymax)
-          val = bp_bilinear_global(d, filtered, k, x, y);
-        float tt = X * v.s + Y * v.c;
-        float dd = fabsf(ts - v.tanb * tt) * v.rs;
-        if (ts < 0.f) dd = -dd;
-        float den = d.D - dd;
-        w = (d.D * d.D) / (den * den);
-      } else {
-        double xd, yd, wd;
-        if (!bp_ref_voxel(d, viewsd[k], s, t, z, &xd, &yd, &wd)) continue;
-        if (xd >= 0.0 && xd <= (double)d.nv && yd >= 0.0 && yd <= (double)d.nu)
-          val = bp_bilinear_global_d(d, filtered, k, xd, yd);
-        w = (float)wd;
-      }
+      int xi, yi;
+      float fx, fy, w;
+      if (!bp_coef(d, v, viewsd[k], s, t, z, X, Y, Z, &xi, &yi, &fx, &fy, &w)) continue;
+      float val = bp_bilinear_at(d, filtered, k, xi, yi, fx, fy);
       acc = fmaf(w * val, v.factor, acc);
     }
   }

@@ -54,7 +54,10 @@ def load(build_if_missing=False):
     lib.monte_fdk_backproject.argtypes = [P, G, P, P, P, C.c_int, C.c_int]
     lib.monte_fdk.argtypes = [P, G, P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.monte_fdk_autotune.argtypes = [P, G, C.POINTER(C.c_int)]
+    lib.monte_fdk_forward_project.argtypes = [P, G, P, P, C.c_int]
+    lib.monte_fdk_backward.argtypes = [P, G, P, P, C.c_int]
     lib.monte_fdk_last_bp_variant.argtypes = [P]
+    lib.monte_fdk_set_bp_variant.argtypes = [P, C.c_int]
     lib.monte_ctx_check_status.argtypes = [P]
     MG = C.POINTER(abi.McGeom)
     lib.monte_mc_geom_reference325.argtypes = [MG]
@@ -67,6 +70,9 @@ def load(build_if_missing=False):
                                  C.POINTER(abi.McStats), C.c_int]
     lib.monte_mc_finalize.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P, P, P,
                                       P, P, P, C.c_int]
+    SG = C.POINTER(abi.SiddonGrid)
+    lib.monte_siddon_forward.argtypes = [P, MG, SG, P, C.c_int, C.c_int, P, P, C.c_int]
+    lib.monte_siddon_backward.argtypes = [P, MG, SG, P, C.c_int, C.c_int, P, P, P, C.c_int]
     _LIB = lib
     return lib
 
@@ -162,6 +168,9 @@ class Context:
     def last_bp_variant(self):
         return self.lib.monte_fdk_last_bp_variant(self.h)
 
+    def set_bp_variant(self, variant):
+        self.check(self.lib.monte_fdk_set_bp_variant(self.h, variant))
+
     # ---- FDK ----------------------------------------------------------
     def fdk_filter(self, g, proj, filtered, mode=abi.MONTE_FILTER_FP32):
         mem = _mem_of(proj, filtered)
@@ -191,6 +200,32 @@ class Context:
         self.check(self.lib.monte_mc_finalize(self.h, n_views, nu, nv, per, _ptr(primary)[0],
                                               _ptr(scatter)[0], _ptr(proj0)[0], _ptr(map0)[0],
                                               _ptr(proj5)[0], _ptr(map5)[0], mem))
+
+    def fdk_forward_project(self, g, vol_xy, out):
+        """Adjoint of fdk_backproject (plain): vol_xy -> out[view][v][u]."""
+        mem = _mem_of(vol_xy, out)
+        self.check(self.lib.monte_fdk_forward_project(self.h, C.byref(g), _ptr(vol_xy)[0],
+                                                      _ptr(out)[0], mem))
+
+    def fdk_backward(self, g, grad_vol, grad_proj):
+        """Adjoint of the whole FDK: grad_vol -> grad_proj[view][u][v]."""
+        mem = _mem_of(grad_vol, grad_proj)
+        self.check(self.lib.monte_fdk_backward(self.h, C.byref(g), _ptr(grad_vol)[0],
+                                               _ptr(grad_proj)[0], mem))
+
+    # ---- primary signal ------------------------------------------------
+    def siddon_forward(self, g, grid, mu, views, line=None, transmission=None):
+        mem = _mem_of(mu, line, transmission)
+        self.check(self.lib.monte_siddon_forward(self.h, C.byref(g), C.byref(grid), _ptr(mu)[0],
+                                                 views[0], views[1], _ptr(line)[0],
+                                                 _ptr(transmission)[0], mem))
+
+    def siddon_backward(self, g, grid, mu, views, grad_mu, grad_line=None, grad_transmission=None):
+        mem = _mem_of(mu, grad_mu, grad_line, grad_transmission)
+        self.check(self.lib.monte_siddon_backward(self.h, C.byref(g), C.byref(grid), _ptr(mu)[0],
+                                                  views[0], views[1], _ptr(grad_line)[0],
+                                                  _ptr(grad_transmission)[0], _ptr(grad_mu)[0],
+                                                  mem))
 
     def fdk(self, g, proj, vol_xy, filtered=None, vol_zy=None,
             filter_mode=abi.MONTE_FILTER_FP32, bp_mode=abi.MONTE_BP_PLAIN):

@@ -49,7 +49,36 @@ def lib():
         _LIB.oracle_logf.argtypes = [f, f, C.c_int]
         _LIB.oracle_sincos_2pi.argtypes = [f, f, f, C.c_int]
         _LIB.oracle_compton.argtypes = [C.c_float, C.c_uint64, C.c_int, f, f]
+        sg = C.POINTER(abi.SiddonGrid)
+        _LIB.oracle_siddon_forward.argtypes = [C.POINTER(abi.McGeom), sg, f, C.c_int, C.c_int, d]
+        _LIB.oracle_siddon_backward.argtypes = [C.POINTER(abi.McGeom), sg, f, C.c_int, C.c_int,
+                                                d, d, d]
     return _LIB
+
+
+def siddon_forward(g, grid, mu, views):
+    """FP64 line integrals [n_views][nu][nv] along the Monte Carlo's
+    emission rays (views outside the range stay 0)."""
+    mu = np.ascontiguousarray(mu, np.float32)
+    out = np.zeros((g.n_views, g.nu, g.nv), np.float64)
+    rc = lib().oracle_siddon_forward(C.byref(g), C.byref(grid), _fp(mu), views[0], views[1],
+                                     _dp(out))
+    if rc != 0:
+        raise ValueError("oracle_siddon_forward rejected the inputs")
+    return out
+
+
+def siddon_backward(g, grid, mu, views, grad_line=None, grad_trans=None):
+    mu = np.ascontiguousarray(mu, np.float32)
+    gm = np.zeros(mu.shape, np.float64)
+    gl = None if grad_line is None else np.ascontiguousarray(grad_line, np.float64)
+    gt = None if grad_trans is None else np.ascontiguousarray(grad_trans, np.float64)
+    rc = lib().oracle_siddon_backward(C.byref(g), C.byref(grid), _fp(mu), views[0], views[1],
+                                      _dp(gl) if gl is not None else None,
+                                      _dp(gt) if gt is not None else None, _dp(gm))
+    if rc != 0:
+        raise ValueError("oracle_siddon_backward rejected the inputs")
+    return gm
 
 
 def mc_run(g, inputs, request):
@@ -149,3 +178,25 @@ def fdk_backproject(g, filtered, z_range=None, zy=False):
     lib().oracle_fdk_backproject(C.byref(g), _fp(filtered), _fp(vol),
                                  _fp(vzy) if zy else None, z0, z1)
     return (vol, vzy) if zy else vol
+
+
+def fdk_forward_project(g, vol64):
+    """FP64 transpose of the FP64 backprojection (no flat-edge quirk)."""
+    vol64 = np.ascontiguousarray(vol64, np.float64)
+    out = np.zeros((g.n_views, g.nv, g.nu), np.float64)
+    L = lib()
+    L.oracle_fdk_forward_project_f64.argtypes = [C.POINTER(FdkGeom), C.POINTER(C.c_double),
+                                                 C.POINTER(C.c_double)]
+    L.oracle_fdk_forward_project_f64(C.byref(g), _dp(vol64), _dp(out))
+    return out
+
+
+def fdk_backward(g, grad_vol64):
+    """FP64 adjoint of the whole FDK: grad_vol -> grad_proj[view][u][v]."""
+    tmp = fdk_forward_project(g, grad_vol64)
+    out = np.zeros((g.n_views, g.nu, g.nv), np.float64)
+    L = lib()
+    L.oracle_fdk_filter_adjoint_f64.argtypes = [C.POINTER(FdkGeom), C.POINTER(C.c_double),
+                                                C.POINTER(C.c_double)]
+    L.oracle_fdk_filter_adjoint_f64(C.byref(g), _dp(tmp), _dp(out))
+    return out

@@ -282,3 +282,82 @@ void oracle_fdk_backproject_f64(const monte_fdk_geom* g, const double* filtered6
   }
   free(views);
 }
+
+/* Transpose of oracle_fdk_backproject_f64 (needs flags without
+ * MONTE_FDK_FLAT_EDGE): out64[view][v][u] = sum over voxels of the same
+ * coefficients times vol64[z][t][s].  FP64 reference for the GPU forward
+ * projector and the FDK gradient. */
+void oracle_fdk_forward_project_f64(const monte_fdk_geom* g, const double* vol64, double* out64) {
+  const int nx = g->nx, ny = g->ny, nu = g->nu, nv = g->nv;
+  bp_view* views = (bp_view*)malloc(sizeof(bp_view) * g->n_views);
+  for (int k = 0; k < g->n_views; k++) bp_view_init(g, k, &views[k]);
+  memset(out64, 0, sizeof(double) * (size_t)g->n_views * nu * nv);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < g->n_views; k++) {
+    const bp_view* v = &views[k];
+    double* out = out64 + (size_t)k * nu * nv;
+    for (int z = 0; z < g->nz; z++)
+      for (int t = 0; t < ny; t++)
+        for (int s = g->s_begin; s < g->s_end; s++) {
+          double r = vol64[(size_t)z * ny * nx + (size_t)t * nx + s];
+          if (r == 0.0) continue;
+          double X = (g->x0 + s * g->dvox), Y = (g->y0 - t * g->dvox), Z = (g->z0 - z * g->dvox);
+          double pv0 = X - v->px, pv1 = Y - v->py, pv2 = Z, tmp_x = pv0;
+          pv0 = pv0 * v->c + pv1 * v->s;
+          pv1 = -tmp_x * v->s + pv1 * v->c;
+          double to_det = g->sdd / pv0;
+          pv1 *= to_det;
+          pv2 *= to_det;
+          if (fabs(pv1) > g->half_u || fabs(pv2) > g->half_v) continue;
+          double y = (g->half_u - pv1) / g->du, x = (g->half_v - pv2) / g->dv;
+          if (!(0 <= x && x <= nv && 0 <= y && y <= nu)) continue;
+          if (g->mask_radius > 0) {
+            int cz = g->nz / 2, ct = g->ny / 2, cs = g->nx / 2;
+            if ((z - cz) * (z - cz) + (t - ct) * (t - ct) + (s - cs) * (s - cs) >
+                g->mask_radius * g->mask_radius)
+              continue;
+          }
+          int yi = (int)y, xi = (int)x;
+          double fx = x - xi, fy = y - yi;
+          double tmp_s = X * v->c - Y * v->s, tmp_t = X * v->s + Y * v->c;
+          double d = fabs(tmp_s - v->tanb * tmp_t) / sqrt(1 + v->tanb * v->tanb);
+          if (tmp_s < 0) d = -d;
+          double D = g->wdist;
+          double dbeta = (360.0 / g->n_views) * 2 * M_PI / 360;
+          double c = D * D / ((D - d) * (D - d)) * dbeta * g->scale * g->scale2 * r;
+          for (int dx = 0; dx < 2; dx++)
+            for (int dy = 0; dy < 2; dy++) {
+              int row = xi + dx, col = yi + dy;
+              if (row >= nv || col >= nu) continue;
+              out[(size_t)row * nu + col] += c * (dx ? fx : 1 - fx) * (dy ? fy : 1 - fy);
+            }
+        }
+  }
+  free(views);
+}
+
+/* Transpose of the weighting + filter (oracle_fdk_filter_f64):
+ * h64[view][u][v] = w(u,v) * sum_b 0.5 h[u-b] g64[view][v][b]. */
+void oracle_fdk_filter_adjoint_f64(const monte_fdk_geom* g, const double* g64, double* h64) {
+  const int nu = g->nu, nv = g->nv;
+  double* taps = (double*)malloc(sizeof(double) * (2 * nu - 1));
+  taps[nu - 1] = 0.25;
+  for (int n = 1; n < nu; n++) {
+    double x = n * M_PI;
+    double v = (n % 2 == 0) ? 0.0 : -1. / (x * x);
+    taps[nu - 1 + n] = v;
+    taps[nu - 1 - n] = v;
+  }
+#pragma omp parallel for schedule(static)
+  for (int n = 0; n < g->n_views; n++) {
+    const double* G = g64 + (size_t)n * nu * nv;
+    double* H = h64 + (size_t)n * nu * nv;
+    for (int c = 0; c < nu; c++)
+      for (int d = 0; d < nv; d++) {
+        double acc = 0.0;
+        for (int b = 0; b < nu; b++) acc += G[(size_t)d * nu + b] * 0.5 * taps[nu - 1 - b + c];
+        H[(size_t)c * nv + d] = acc * fdk_weight(g, c, d);
+      }
+  }
+  free(taps);
+}

@@ -21,6 +21,8 @@ def ctx():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from monte_gb300.lib import Context
-    c = Context(0)
+    # share torch's stream, so library work and torch ops on its tensors are
+    # ordered without extra synchronisation
+    c = Context(0, stream=torch.cuda.current_stream())
     yield c
     c.close()
