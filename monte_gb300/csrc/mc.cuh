@@ -23,6 +23,14 @@ struct McDev {
 };
 
 cudaError_t launch_mc(const McDev& d, int kernel, int sm_count, cudaStream_t st);
+
+// Jobs one batched persistent launch can carry.
+constexpr int kMaxBatchJobs = 1024;
+// One persistent launch over the histories of n_jobs jobs; starts[j] is the
+// first global history of job j, starts[n_jobs] = total (device arrays).
+cudaError_t launch_mc_batch(const McDev* jobs, const unsigned long long* starts, int n_jobs,
+                            unsigned long long total, unsigned long long* counter,
+                            unsigned long long* stats, int sm_count, cudaStream_t st);
 cudaError_t launch_mc_finalize(size_t n, unsigned long long per, double log_per,
                                const long long* prim, const long long* scat, int* proj0,
                                float* map0, int* proj5, float* map5, cudaStream_t st);

@@ -180,6 +180,106 @@ __global__ void __launch_bounds__(256) mc_persistent_kernel(McDev d) {
   warp_stats(d, st);
 }
 
+// The persistent kernel over the histories of many jobs (phantoms of their
+// own size, geometry and tables): the global history counter runs over the
+// concatenated history ranges, and a lane that takes history h finds its
+// job by binary search over the range starts.  Everything else is the
+// single-job kernel's loop, reading the job's parameters through a pointer.
+__global__ void __launch_bounds__(256) mc_persistent_batch_kernel(
+    const McDev* __restrict__ jobs, const unsigned long long* __restrict__ starts, int n_jobs,
+    unsigned long long total, unsigned long long* counter, unsigned long long* stats) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  __shared__ unsigned long long s_starts[kMaxBatchJobs + 1];
+  for (int i = threadIdx.x; i <= n_jobs; i += blockDim.x) s_starts[i] = starts[i];
+  __syncthreads();
+  unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
+  mc_photon p;
+  p.state = MC_DEAD;
+  p.n_int = 0;
+  const McDev* J = jobs;
+  bool retired = false;
+  unsigned long long pool_next = 0, pool_end = 0;
+  while (true) {
+    const unsigned need = __ballot_sync(FULL, p.state == MC_DEAD && !retired);
+    if (need) {
+      const unsigned cnt = __popc(need);
+      const unsigned rank = __popc(need & lt_mask);
+      const unsigned long long avail = pool_end - pool_next;
+      unsigned long long base = 0;
+      if (avail < cnt) {
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)kChunk);
+        base = __shfl_sync(FULL, base, 0);
+      }
+      if (need & (1u << lane)) {
+        unsigned long long h = rank < avail ? pool_next + rank : base + (rank - avail);
+        if (h >= total) {
+          retired = true;
+        } else {
+          int lo = 0, hi = n_jobs - 1;  // last job whose start <= h
+          while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (s_starts[mid] <= h) lo = mid; else hi = mid - 1;
+          }
+          J = jobs + lo;
+          int view, iu, iv;
+          unsigned long long k;
+          decompose(*J, h - s_starts[lo], &view, &iu, &iv, &k);
+          st[2] += (unsigned long long)p.n_int;
+          mc_start(&J->P, J->T, J->V, J->U, J->W, view, iu, iv, k, &p);
+          st[0]++;
+        }
+      }
+      if (avail >= cnt) {
+        pool_next += cnt;
+      } else {
+        pool_next = base + (cnt - avail);
+        pool_end = base + kChunk;
+        if (pool_end > total) pool_end = total;
+        if (pool_next > pool_end) pool_next = pool_end;
+      }
+    }
+    if (__all_sync(FULL, retired)) break;
+#pragma unroll 1
+    for (int i = 0; i < kStepsPerRound && p.state == MC_FLY; i++) {
+      mc_flight_step(&J->P, J->T, J->labels, &p);
+      st[1]++;
+      if (p.state == MC_DEAD) st[5]++;
+    }
+    long long cell = -1;
+    int kind = 0;
+    if (p.state == MC_ESCAPED) {
+      kind = mc_tally_kind(&J->P, &p);
+      cell = mc_detector_index(&J->P, J->V, &p);
+      if (kind < 0) cell = -1;
+      p.state = MC_DEAD;
+    }
+    // group lanes by (job, tally, pixel)
+    unsigned long long* dst = nullptr;
+    if (cell >= 0) dst = (kind == 0 ? J->prim : J->scat) + cell;
+    const unsigned tal = __ballot_sync(FULL, dst != nullptr);
+    if (dst) {
+      const unsigned grp = __match_any_sync(tal, (unsigned long long)dst);
+      if (lane == __ffs(grp) - 1) atomicAdd(dst, (unsigned long long)__popc(grp));
+      st[3 + kind]++;
+    }
+    const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
+    const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
+    if (coll && (__popc(coll) >= kCollideBatch || fly == 0)) {
+      if (p.state == MC_COLLIDED) p.state = mc_after_collision(&J->P, J->T, &p);
+    }
+  }
+  st[2] += (unsigned long long)p.n_int;
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    unsigned long long x = st[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    if (lane == 0 && x) atomicAdd(&stats[i], x);
+  }
+}
+
 __global__ void mc_finalize_kernel(size_t n, unsigned long long per, double log_per,
                                    const long long* __restrict__ prim,
                                    const long long* __restrict__ scat, int* __restrict__ proj0,
@@ -215,6 +315,20 @@ cudaError_t launch_mc(const McDev& d, int kernel, int sm_count, cudaStream_t st)
     if (per_sm < 1) per_sm = 1;
     mc_persistent_kernel<<<sm_count * per_sm, 256, 0, st>>>(d);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mc_batch(const McDev* jobs, const unsigned long long* starts, int n_jobs,
+                            unsigned long long total, unsigned long long* counter,
+                            unsigned long long* stats, int sm_count, cudaStream_t st) {
+  if (n_jobs <= 0 || n_jobs > kMaxBatchJobs) return cudaErrorInvalidValue;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_persistent_batch_kernel,
+                                                                256, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  mc_persistent_batch_kernel<<<sm_count * per_sm, 256, 0, st>>>(jobs, starts, n_jobs, total,
+                                                                counter, stats);
   return cudaGetLastError();
 }
 

@@ -27,29 +27,35 @@ struct SiddonGrid {
 template <typename F>
 __device__ __forceinline__ void siddon_walk(const SiddonGrid& g, float ox, float oy, float oz,
                                             float dx, float dy, float dz, F&& f) {
-  const float inv[3] = {1.0f / g.dx, 1.0f / g.dy, 1.0f / g.dz};
-  const float o[3] = {(ox - g.x0) * inv[0], (oy - g.y0) * inv[1], (oz - g.z0) * inv[2]};
-  const float dir[3] = {dx * inv[0], dy * inv[1], dz * inv[2]};
+  // Per-ray set-up in double: the source sits hundreds of voxels from the
+  // grid, and in float the entry point (a small difference of large
+  // numbers) would shift the ray by ~1e-5 voxel -- enough to move the plane
+  // crossings of rays that graze a plane.  The walk itself runs in float
+  // from the entry point, where all parameters stay within the grid's extent.
+  const double invd[3] = {1.0 / (double)g.dx, 1.0 / (double)g.dy, 1.0 / (double)g.dz};
+  const double od[3] = {((double)ox - (double)g.x0) * invd[0], ((double)oy - (double)g.y0) * invd[1],
+                        ((double)oz - (double)g.z0) * invd[2]};
+  const double dd[3] = {(double)dx * invd[0], (double)dy * invd[1], (double)dz * invd[2]};
   const int n[3] = {g.nx, g.ny, g.nz};
-  float t0 = 0.0f, t1 = 3.0e38f;
+  double t0d = 0.0, t1d = 1.0e300;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    if (dir[a] == 0.0f) {
-      if (o[a] < 0.0f || o[a] >= (float)n[a]) return;
+    if (dd[a] == 0.0) {
+      if (od[a] < 0.0 || od[a] >= (double)n[a]) return;
     } else {
-      float ta = (0.0f - o[a]) / dir[a], tb = ((float)n[a] - o[a]) / dir[a];
-      t0 = fmaxf(t0, fminf(ta, tb));
-      t1 = fminf(t1, fmaxf(ta, tb));
+      double ta = -od[a] / dd[a], tb = ((double)n[a] - od[a]) / dd[a];
+      t0d = fmax(t0d, fmin(ta, tb));
+      t1d = fmin(t1d, fmax(ta, tb));
     }
   }
-  if (!(t0 < t1)) return;
-  // Re-origin at the grid entry point: parameters measured from the source
-  // (tens of cm) would leave only ~1e-5 relative precision in each segment
-  // length; from the entry point they stay within the grid's own extent.
-  float e[3];
+  if (!(t0d < t1d)) return;
+  float e[3], dir[3];
 #pragma unroll
-  for (int a = 0; a < 3; a++) e[a] = fmaf(t0, dir[a], o[a]);
-  t1 -= t0;
+  for (int a = 0; a < 3; a++) {
+    e[a] = (float)(od[a] + t0d * dd[a]);
+    dir[a] = (float)dd[a];
+  }
+  float t1 = (float)(t1d - t0d);
   // voxel at the entry: evaluate 1e-4 voxel inside the grid
   int idx[3], step[3];
   float tnext[3];
