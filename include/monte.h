@@ -305,6 +305,32 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
                  const monte_xcom* xcom, const monte_spectrum* spec, const monte_mc_request* run,
                  int64_t* primary, int64_t* scatter, monte_mc_stats* stats, int mem);
 
+/* Limits of monte_mc_run_noalloc's static scratch. */
+#define MONTE_NOALLOC_MAX_VIEWS  1024
+#define MONTE_NOALLOC_MAX_PIXELS 1024
+
+/* monte_mc_run for callers that cannot allocate device memory -- a service
+ * that reserves all of the GPU's memory for its own pool, a framework whose
+ * allocator must own every device allocation, a latency-critical loop where
+ * a cudaMalloc (which can synchronize the device) is not acceptable.  It has
+ * no counterpart in the reference.  It needs no context and allocates
+ * nothing: the tables, the history counter and the statistics live in a
+ * static device array of about 280 KB that every GPU loading the library
+ * holds until exit.  Same semantics as monte_mc_run with the persistent or
+ * plain kernel, on the current device and `cuda_stream` (NULL: the legacy
+ * default stream); labels, primary and scatter must be device pointers.
+ * Requests with more than MONTE_NOALLOC_MAX_VIEWS views or
+ * MONTE_NOALLOC_MAX_PIXELS pixels along an axis are rejected (MONTE_EINVAL).
+ * The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress); make it before any stream capture.  All calls on a
+ * device share the array, which keeps the last call's contents: calls whose
+ * work overlaps on the GPU race and must be serialized.  If stats is not
+ * NULL the call waits for the stream.  Errors: monte_last_error(NULL). */
+int monte_mc_run_noalloc(const monte_mc_geom* g, const monte_mc_phantom* ph,
+                         const monte_xcom* xcom, const monte_spectrum* spec,
+                         const monte_mc_request* run, int64_t* primary, int64_t* scatter,
+                         monte_mc_stats* stats, void* cuda_stream);
+
 /* Reference post-processing (monte_cu/CBCT_real325im.cu:261-294): counts
  * clamped to [1, per]; map = -ln N + ln(per).  proj0/map0 from the primary
  * tally, proj5/map5 from primary + scatter; any output may be NULL.  All
