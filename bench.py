@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form FDK timing")
     ap.add_argument("--no-mc", action="store_true", help="skip the Monte Carlo timing")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-scan timing")
+    ap.add_argument("--batch-scale", type=float, default=0.1,
+                    help="histories per view of the batched scans, as a fraction of 1e6-1e7")
     ap.add_argument("--tile", type=int, default=-1,
                     help="backprojection tile shape (default: autotune)")
     ap.add_argument("--small", action="store_true", help="reduced sizes (for profiling runs)")
@@ -79,22 +82,32 @@ class Clocks:
         self.proc = None
         self.lines = []
 
+    INTERVAL_MS = 50
+
     def start(self):
+        """Start sampling and wait (up to 3 s) for the first sample, so that
+        the region timed next is covered from its start."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200", "-i", str(self.dev)],
+                 "-lms", str(self.INTERVAL_MS), "-i", str(self.dev)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t = time.time()
+        while not self.lines and time.time() - t < 3.0:
+            time.sleep(0.01)
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.time(), ln.strip()))
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """Summary of the samples taken in the host-time window [t0, t1]
+        (plus one sampling interval), or of all samples."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -105,7 +118,11 @@ class Clocks:
         self.th.join(timeout=2)
         sm, smax, reasons, power = [], [], set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if t0 is not None:
+            window = [x for x in lines if t0 <= x[0] <= t1 + self.INTERVAL_MS / 1e3]
+            lines = window or [x for x in lines if x[0] >= t0][:1]
+        for _, ln in lines:
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 9:
                 continue
@@ -233,6 +250,58 @@ def mc_bench(ctx, device, steps=3, per=509):
     return out
 
 
+BATCH_WORKLOAD = ("batch: 64 scans, cube phantoms of side U{65..257} at 0.8 mm (ellipsoids of "
+                  "water / Ca-water bone 1.5-1.9 in air), views U{60..360}, detector nu in "
+                  "{128..512 step 64} x nv in {128, 256, 384}, 20-80 keV lines weighted "
+                  "(80-E), Monte Carlo then FDK of the total map into side^3")
+
+
+def batch_bench(ctx, device, scale):
+    """Wall time of the whole 64-scan batch: FUSED (one persistent Monte
+    Carlo launch + per-scan BF16x3 filter and autotuned tiled backprojection,
+    one CUDA graph) against SEQUENTIAL (64 x plain Monte Carlo, finalize,
+    FP32 filter, plain backprojection).  Histories per view are the drawn
+    1e6-1e7 times `scale`."""
+    import torch
+    from monte_gb300 import abi, batchscan
+    x = np.load(os.path.join(REPO, "tests", "golden", "xcom.npz"))
+    b = batchscan.Batch(batchscan.specs(hist_scale=scale), x["water"], x["ca"], device=device)
+    H, U = b.histories(), b.updates()
+    out = {"workload": BATCH_WORKLOAD, "hist_per_view_scale": scale, "histories": H,
+           "voxel_view_updates": U}
+    stream = torch.cuda.current_stream(device)
+
+    def timed(plan, reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        for _ in range(reps):
+            plan.run()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    for name, mode, opts, warm in (("fused", abi.MONTE_BATCH_FUSED, abi.MONTE_BATCH_AUTOTUNE, 1),
+                                   ("sequential", abi.MONTE_BATCH_SEQUENTIAL, 0, 0)):
+        t0 = time.time()
+        plan = ctx.batch(b.xcom, b.jobs, mode=mode, options=opts)
+        torch.cuda.synchronize(device)
+        create_s = time.time() - t0
+        for _ in range(warm):
+            plan.run()
+        t = timed(plan, 1)
+        st = plan.stats()
+        ctx.check_status()
+        out[name] = {"s_per_batch": t, "histories_per_s": H / t, "gups": U / t / 1e9,
+                     "create_s": create_s, "dropped": st["dropped"]}
+        if name == "fused":
+            out[name]["bp_variants"] = sorted({plan.bp_variant(j) for j in range(len(b.jobs))})
+        plan.close()
+    out["fused_over_sequential"] = out["sequential"]["s_per_batch"] / out["fused"]["s_per_batch"]
+    return out
+
+
 def run_reference(args):
     world, rank, local = dist_setup(args)
     if rank != 0:
@@ -292,14 +361,15 @@ def run_ours(args):
         ctx.fdk_filter(g, proj, filt, mode=fmode)
         ctx.fdk_backproject(g, filt, vol, mode=bmode)
 
+    clocks = Clocks(local)
+    clocks.start()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize(dev)
-    clocks = Clocks(local)
-    clocks.start()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize(dev)
+    h0 = time.time()
     t_all0 = torch.cuda.Event(enable_timing=True)
     t_all1 = torch.cuda.Event(enable_timing=True)
     t_all0.record(stream)
@@ -311,8 +381,9 @@ def run_ours(args):
         ev[i][2].record(stream)
     t_all1.record(stream)
     torch.cuda.synchronize(dev)
+    h1 = time.time()
     barrier(world)
-    clk = clocks.stop()
+    clk = clocks.stop(h0, h1)
     elapsed = t_all0.elapsed_time(t_all1) / 1e3
     elapsed = max_over_ranks(elapsed, world, dev)
     t_filter = statistics.mean(e[0].elapsed_time(e[1]) for e in ev) / 1e3
@@ -404,6 +475,8 @@ def run_ours(args):
     if not args.no_mc:
         line["mc"] = mc_bench(ctx, dev)
         line["gpu_launches_mc"] = 2 * 4
+    if not args.no_batch and not args.small:
+        line["batch"] = batch_bench(ctx, dev, args.batch_scale)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g)
     if rank == 0:

@@ -340,6 +340,70 @@ int monte_mc_finalize(monte_ctx* ctx, int32_t n_views, int32_t nu, int32_t nv, u
                       float* map0, int32_t* proj5, float* map5, int mem);
 
 /* ======================================================================
+ *  Batched scans (serving-style)
+ * ====================================================================== */
+
+/*
+ * One simulated scan of a batch: the Monte Carlo of a phantom (the
+ * projection launch plus post-processing of monte_cu/CBCT_real325im.cu:
+ * 235-294), then the FDK reconstruction of its -log map
+ * (recon/bp3d20.cpp:15-194), which reads the map as proj[view][u][v].  The
+ * reference runs one phantom per program invocation; the batch has no
+ * counterpart there.
+ *
+ * fdk.n_views, fdk.nu, fdk.nv must equal mc.n_views, mc.nu, mc.nv.  The
+ * labels and every output are device pointers.  History streams are those of
+ * monte_mc_run with request {seed, histories_per_pixel, all views and
+ * pixels, job = the job's index in the batch}.
+ */
+typedef struct monte_batch_job {
+  monte_mc_geom mc;
+  monte_mc_phantom phantom;
+  monte_spectrum spectrum;
+  uint64_t seed;
+  uint64_t histories_per_pixel;
+  monte_fdk_geom fdk;
+  int32_t recon_total;      /* 0: reconstruct map0 (primary only),
+                               1: map5 (primary + scatter) */
+  int32_t reserved0;
+  int64_t* primary;         /* [n_views][nu][nv] tallies, zeroed by every run */
+  int64_t* scatter;
+  float* map;               /* [n_views][nu][nv] map the FDK reads; NULL: plan-owned */
+  float* vol_xy;            /* [nz][ny][nx] reconstruction */
+} monte_batch_job;
+
+/* Batch execution forms. */
+#define MONTE_BATCH_FUSED      0 /* one persistent Monte Carlo launch over the
+                                    histories of all jobs, then per job finalize,
+                                    split-BF16 tensor-core filter (FP32 where the
+                                    detector does not fit it) and tiled
+                                    backprojection, the jobs spread over four
+                                    streams; all captured once in a CUDA graph */
+#define MONTE_BATCH_SEQUENTIAL 1 /* per job, one after another: plain Monte
+                                    Carlo kernel, finalize, FP32 filter, plain
+                                    backprojection (no graph) */
+/* monte_batch_create option bits. */
+#define MONTE_BATCH_AUTOTUNE 0x1 /* time the tile shapes of the tiled
+                                    backprojector on every distinct FDK
+                                    geometry at creation (FUSED only) */
+
+typedef struct monte_batch monte_batch;
+
+/* Validate the jobs, build and upload every table, allocate the plan's
+ * device memory and, for MONTE_BATCH_FUSED, capture the CUDA graph.  The
+ * job array is copied; the buffers it points at must outlive the plan.
+ * xcom is shared by all jobs.  At most 1024 jobs. */
+int monte_batch_create(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* jobs,
+                       int n_jobs, int mode, int options, monte_batch** out);
+/* Queue one run of the whole batch on the context's stream (asynchronous). */
+int monte_batch_run(monte_batch* b);
+/* Statistics of the last run (waits for the context's stream). */
+int monte_batch_stats(monte_batch* b, monte_mc_stats* stats);
+/* Tile shape the backprojection of job j runs with (-1: plain kernel). */
+int monte_batch_bp_variant(const monte_batch* b, int job);
+int monte_batch_destroy(monte_batch* b);
+
+/* ======================================================================
  *  Primary signal (differentiable mode)
  * ====================================================================== */
 

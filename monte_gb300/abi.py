@@ -289,6 +289,30 @@ def mc_request(seed, per, views, u_range, v_range, kernel=MONTE_MC_PERSISTENT, j
     return r
 
 
+MONTE_BATCH_FUSED = 0
+MONTE_BATCH_SEQUENTIAL = 1
+MONTE_BATCH_AUTOTUNE = 0x1
+
+
+class BatchJob(C.Structure):
+    """monte_batch_job."""
+
+    _fields_ = [
+        ("mc", McGeom),
+        ("phantom", McPhantom),
+        ("spectrum", McSpectrum),
+        ("seed", C.c_uint64),
+        ("histories_per_pixel", C.c_uint64),
+        ("fdk", FdkGeom),
+        ("recon_total", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("primary", C.c_void_p),
+        ("scatter", C.c_void_p),
+        ("map", C.c_void_p),
+        ("vol_xy", C.c_void_p),
+    ]
+
+
 class SiddonGrid(C.Structure):
     """monte_siddon_grid."""
 

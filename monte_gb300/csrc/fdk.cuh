@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 
 #include "../../include/monte.h"
 
@@ -41,10 +42,40 @@ struct FdkDev {
   float sdd, D, sod;
   float half_u, half_v;
   float inv_du, inv_dv;
+  // low parts of 1/du, 1/dv and dvox/dv (value - float(value)): a float
+  // reciprocal pitch alone is a ~6e-8 scale error of every detector
+  // coordinate, ~1e-5 pixel at column 128
+  float inv_du_lo, inv_dv_lo;
+  float dvox_inv_dv, dvox_inv_dv_lo;
   float xmax, ymax;      // accepted detector coordinate ranges [0,xmax], [0,ymax]
 };
 
+// (h - p) / pitch as (h - p) * (inv_hi + inv_lo), the product rounded once.
+__host__ __device__ __forceinline__ float bp_scale(float t, float inv_hi, float inv_lo) {
+  return fmaf(t, inv_hi, t * inv_lo);
+}
+
 FdkDev make_fdk_dev(const monte_fdk_geom& g);
+
+// Host copies of the per-geometry tables (fdk_api.cu): view constants in
+// float and double, cosine weights [u][v], taps 0.5*h, and the pre-split
+// Toeplitz operand of the tensor-core filter (empty if that filter does not
+// fit the geometry).
+struct FdkHostTables {
+  std::vector<BpView> views;
+  std::vector<BpViewD> viewsd;
+  std::vector<float> weights;
+  std::vector<float> taps;
+  std::vector<uint16_t> bsplit;
+};
+void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t);
+// Argument checks of the FDK entry points (sets the context's error text).
+int fdk_validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid);
+// Time every tiled backprojector shape that fits g (three launches each on
+// the context's stream, the first discarded) into scratch `dv` from
+// filtered projections `df`; *best = fastest shape, -1 if none fits.
+int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
+                const BpViewD* viewsd, const float* df, float* dv, int* best);
 
 // Kernel launchers (return cudaGetLastError()).
 cudaError_t launch_fdk_filter_fp32(const FdkDev& d, const float* proj, const float* weights,
@@ -165,16 +196,28 @@ __device__ __forceinline__ bool bp_near_edge(const FdkDev& d, float ts, float up
 // outside the interpolation guard of :152).  The plain backprojector and
 // its adjoint (the forward projector) both use this function, so the two
 // are exact transposes of each other.
+// Voxel (X, Y) in the frame of view v: Vx along the central ray from the
+// source, Vy across it.  The reference forms (X - px) c + (Y - py) s and
+// (Y - py) c - (X - px) s in double (recon/bp3d20.cpp:103-110); with the
+// source at px = -sod c, py = -sod s these equal X c + Y s + sod and
+// Y c - X s exactly.  Written so, the sod-sized source terms never cancel in
+// float: the detector column keeps ~1e-6 pixel accuracy where the
+// difference form loses ~1e-4 pixel at fine detector pitch.
+__device__ __forceinline__ void bp_view_frame(const FdkDev& d, const BpView& v, float X, float Y,
+                                              float* Vx, float* Vy) {
+  *Vx = fmaf(X, v.c, Y * v.s) + d.sod;
+  *Vy = fmaf(Y, v.c, -(X * v.s));
+}
+
 __device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const BpViewD& vd, int s,
                                         int t, int z, float X, float Y, float Z, int* xi, int* yi,
                                         float* fx, float* fy, float* w) {
-  float ax = X - v.px, ay = Y - v.py;
-  float Vx = ax * v.c + ay * v.s;
-  float Vy = ay * v.c - ax * v.s;
+  float Vx, Vy;
+  bp_view_frame(d, v, X, Y, &Vx, &Vy);
   float kk = d.sdd / Vx;
   float up = Vy * kk, vp = Z * kk;
-  float y = (d.half_u - up) * d.inv_du;
-  float x = (d.half_v - vp) * d.inv_dv;
+  float y = bp_scale(d.half_u - up, d.inv_du, d.inv_du_lo);
+  float x = bp_scale(d.half_v - vp, d.inv_dv, d.inv_dv_lo);
   float ts = X * v.c - Y * v.s;
   if (!bp_near_edge(d, ts, up, vp, x, y)) {
     if (fabsf(up) > d.half_u || fabsf(vp) > d.half_v) return false;

@@ -79,9 +79,8 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
       const float Y = fmaf(-(float)t, d.dvox, d.y0);
       // cheap column test: does this voxel column project near our columns?
       {
-        float ax = X - v.px, ay = Y - v.py;
-        float Vx = ax * v.c + ay * v.s;
-        float Vy = ay * v.c - ax * v.s;
+        float Vx, Vy;
+        bp_view_frame(d, v, X, Y, &Vx, &Vy);
         float y = (d.half_u - Vy * (d.sdd / Vx)) * d.inv_du;
         if (!(y >= (float)(c0 - 2) && y < (float)(c0 + ncols + 1))) continue;
       }

@@ -51,6 +51,10 @@ FdkDev make_fdk_dev(const monte_fdk_geom& g) {
   d.half_v = (float)g.half_v;
   d.inv_du = (float)(1.0 / g.du);
   d.inv_dv = (float)(1.0 / g.dv);
+  d.inv_du_lo = (float)(1.0 / g.du - (double)d.inv_du);
+  d.inv_dv_lo = (float)(1.0 / g.dv - (double)d.inv_dv);
+  d.dvox_inv_dv = (float)(g.dvox / g.dv);
+  d.dvox_inv_dv_lo = (float)(g.dvox / g.dv - (double)d.dvox_inv_dv);
   // recon/bp3d20.cpp:116 rejects |u'|>half_u, |v'|>half_v; :152 then needs
   // 0 <= x <= nv and 0 <= y <= nu.
   d.xmax = (float)std::fmin((double)g.nv, 2.0 * g.half_v / g.dv);
@@ -58,9 +62,7 @@ FdkDev make_fdk_dev(const monte_fdk_geom& g) {
   return d;
 }
 
-namespace {
-
-int validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid) {
+int fdk_validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid) {
   if (!g) return set_error(ctx, MONTE_EINVAL, "geometry is NULL");
   if (g->n_views <= 0 || g->nu <= 0 || g->nv <= 0)
     return set_error(ctx, MONTE_EINVAL, "bad detector size views=%d nu=%d nv=%d", g->n_views,
@@ -90,14 +92,12 @@ int validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid) {
   return MONTE_OK;
 }
 
-// Upload per-view constants, weight table and taps for geometry g (cached).
-int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
-  std::vector<uint8_t> key(sizeof(monte_fdk_geom));
-  memcpy(key.data(), g, sizeof(monte_fdk_geom));
-  if (key == ctx->fdk_key && ctx->fdk_views.ptr) return MONTE_OK;
+void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t) {
   const int nv_ = g->n_views, nu = g->nu, nv = g->nv;
-  std::vector<BpView> views(nv_);
-  std::vector<BpViewD> viewsd(nv_);
+  std::vector<BpView>& views = t->views;
+  std::vector<BpViewD>& viewsd = t->viewsd;
+  views.assign(nv_, BpView());
+  viewsd.assign(nv_, BpViewD());
   float beta_span = (float)(360.0 / nv_);
   for (int k = 0; k < nv_; k++) {
     double beta = (double)k * 360.0 / nv_;
@@ -121,7 +121,8 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
     viewsd[k].tanb = tanb;
   }
   // cosine weights w[u][v] (recon/bp3d20.cpp:40)
-  std::vector<float> w((size_t)nu * nv);
+  std::vector<float>& w = t->weights;
+  w.assign((size_t)nu * nv, 0.f);
   for (int a = 0; a < nu; a++)
     for (int b = 0; b < nv; b++) {
       double D = g->wdist;
@@ -130,7 +131,8 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
       w[(size_t)a * nv + b] = (float)(D / sqrt(D * D + pu * pu + pv * pv));
     }
   // taps 0.5*h[n] at index nu-1+n (recon/bp3d20.cpp:48-60,68)
-  std::vector<float> taps(2 * nu - 1);
+  std::vector<float>& taps = t->taps;
+  taps.assign(2 * nu - 1, 0.f);
   taps[nu - 1] = 0.125f;
   for (int n = 1; n < nu; n++) {
     float h = 0.f;
@@ -140,6 +142,62 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
     }
     taps[nu - 1 + n] = taps[nu - 1 - n] = 0.5f * h;
   }
+  t->bsplit.clear();
+  if (bf16x3_supported(make_fdk_dev(*g))) {
+    t->bsplit.resize(bf16x3_bsplit_bytes(nu) / 2);
+    bf16x3_build_bsplit(nu, taps.data(), t->bsplit.data());
+  }
+}
+
+int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
+                const BpViewD* viewsd, const float* df, float* dv, int* best) {
+  FdkDev d = make_fdk_dev(*g);
+  cudaEvent_t e0, e1;
+  MONTE_CUDA(ctx, cudaEventCreate(&e0));
+  MONTE_CUDA(ctx, cudaEventCreate(&e1));
+  int pick = -1;
+  float best_ms = 3.0e38f;
+  for (int v = 0; v < fdk_bp_tiled_variants(); v++) {
+    if (!fdk_bp_tiled_supported(d, v)) continue;
+    float ms_min = 3.0e38f;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, ctx->stream);
+      cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, dv, nullptr, v, ctx->d_status,
+                                          ctx->stream);
+      cudaEventRecord(e1, ctx->stream);
+      if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(ctx, e != cudaSuccess ? e : cudaGetLastError(), "autotune launch");
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0 && ms < ms_min) ms_min = ms;  // first run warms up
+    }
+    if (ms_min < best_ms) {
+      best_ms = ms_min;
+      pick = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *best = pick;
+  return MONTE_OK;
+}
+
+namespace {
+
+// Upload per-view constants, weight table and taps for geometry g (cached).
+int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
+  std::vector<uint8_t> key(sizeof(monte_fdk_geom));
+  memcpy(key.data(), g, sizeof(monte_fdk_geom));
+  if (key == ctx->fdk_key && ctx->fdk_views.ptr) return MONTE_OK;
+  FdkHostTables t;
+  build_fdk_tables(g, &t);
+  const std::vector<BpView>& views = t.views;
+  const std::vector<BpViewD>& viewsd = t.viewsd;
+  const std::vector<float>& w = t.weights;
+  const std::vector<float>& taps = t.taps;
   MONTE_TRY(ensure(ctx, ctx->fdk_views, views.size() * sizeof(BpView), "view table"));
   MONTE_TRY(ensure(ctx, ctx->fdk_viewsd, viewsd.size() * sizeof(BpViewD), "view table"));
   MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_viewsd.ptr, viewsd.data(),
@@ -153,11 +211,9 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
                                   cudaMemcpyHostToDevice, ctx->stream));
   MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_taps.ptr, taps.data(), taps.size() * sizeof(float),
                                   cudaMemcpyHostToDevice, ctx->stream));
-  if (bf16x3_supported(make_fdk_dev(*g))) {
-    std::vector<uint16_t> bs(bf16x3_bsplit_bytes(nu) / 2);
-    bf16x3_build_bsplit(nu, taps.data(), bs.data());
-    MONTE_TRY(ensure(ctx, ctx->fdk_bsplit, bs.size() * 2, "split Toeplitz operand"));
-    MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_bsplit.ptr, bs.data(), bs.size() * 2,
+  if (!t.bsplit.empty()) {
+    MONTE_TRY(ensure(ctx, ctx->fdk_bsplit, t.bsplit.size() * 2, "split Toeplitz operand"));
+    MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->fdk_bsplit.ptr, t.bsplit.data(), t.bsplit.size() * 2,
                                     cudaMemcpyHostToDevice, ctx->stream));
   }
   // the host vectors die at return: make the copies complete first
@@ -272,7 +328,7 @@ void monte_fdk_geom_reference325(monte_fdk_geom* g) {
 int monte_fdk_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
                      int filter_mode, int mem) {
   if (!ctx) return MONTE_EINVAL;
-  MONTE_TRY(validate(ctx, g, false));
+  MONTE_TRY(fdk_validate(ctx, g, false));
   if (!proj || !filtered) return set_error(ctx, MONTE_EINVAL, "null projection/filtered pointer");
   if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
     return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
@@ -294,7 +350,7 @@ int monte_fdk_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
 int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* filtered,
                           float* vol_xy, float* vol_zy, int bp_mode, int mem) {
   if (!ctx) return MONTE_EINVAL;
-  MONTE_TRY(validate(ctx, g, true));
+  MONTE_TRY(fdk_validate(ctx, g, true));
   if (!filtered || !vol_xy) return set_error(ctx, MONTE_EINVAL, "null filtered/volume pointer");
   if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
     return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
@@ -319,7 +375,7 @@ int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* 
 int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
               float* vol_xy, float* vol_zy, int filter_mode, int bp_mode, int mem) {
   if (!ctx) return MONTE_EINVAL;
-  MONTE_TRY(validate(ctx, g, true));
+  MONTE_TRY(fdk_validate(ctx, g, true));
   if (!proj || !vol_xy) return set_error(ctx, MONTE_EINVAL, "null projection/volume pointer");
   if (mem != MONTE_MEM_DEVICE && mem != MONTE_MEM_HOST)
     return set_error(ctx, MONTE_EINVAL, "bad mem %d", mem);
@@ -356,10 +412,9 @@ int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float*
 
 int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
   if (!ctx) return MONTE_EINVAL;
-  MONTE_TRY(validate(ctx, g, true));
+  MONTE_TRY(fdk_validate(ctx, g, true));
   MONTE_TRY(enter(ctx));
   MONTE_TRY(prepare_tables(ctx, g));
-  FdkDev d = make_fdk_dev(*g);
   const size_t pb = proj_bytes(g), vb = vol_bytes(g);
   MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "autotune filtered"));
   MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "autotune volume"));
@@ -368,35 +423,8 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
   float* dv = (float*)ctx->scratch[kScratchVolXY].ptr;
   const BpView* views = (const BpView*)ctx->fdk_views.ptr;
   const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
-  cudaEvent_t e0, e1;
-  MONTE_CUDA(ctx, cudaEventCreate(&e0));
-  MONTE_CUDA(ctx, cudaEventCreate(&e1));
   int pick = -1;
-  float best_ms = 3.0e38f;
-  for (int v = 0; v < fdk_bp_tiled_variants(); v++) {
-    if (!fdk_bp_tiled_supported(d, v)) continue;
-    float ms_min = 3.0e38f;
-    for (int rep = 0; rep < 3; rep++) {
-      cudaEventRecord(e0, ctx->stream);
-      cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, dv, nullptr, v, ctx->d_status,
-                                          ctx->stream);
-      cudaEventRecord(e1, ctx->stream);
-      if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        return cuda_fail(ctx, e != cudaSuccess ? e : cudaGetLastError(), "autotune launch");
-      }
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (rep > 0 && ms < ms_min) ms_min = ms;  // first run warms up
-    }
-    if (ms_min < best_ms) {
-      best_ms = ms_min;
-      pick = v;
-    }
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick));
   ctx->bp_tune_choice = pick;
   if (best) *best = pick;
   return monte_ctx_check_status(ctx);
@@ -407,7 +435,7 @@ int monte_fdk_last_bp_variant(const monte_ctx* ctx) { return ctx ? ctx->last_bp_
 int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const float* vol_xy,
                               float* filtered_out, int mem) {
   if (!ctx) return MONTE_EINVAL;
-  MONTE_TRY(validate(ctx, g, true));
+  MONTE_TRY(fdk_validate(ctx, g, true));
   if (!vol_xy || !filtered_out) return set_error(ctx, MONTE_EINVAL, "null volume/output pointer");
   if (g->flags & MONTE_FDK_FLAT_EDGE)
     return set_error(ctx, MONTE_EUNSUPPORTED,
@@ -442,7 +470,7 @@ int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const flo
 int monte_fdk_backward(monte_ctx* ctx, const monte_fdk_geom* g, const float* grad_vol,
                        float* grad_proj, int mem) {
   if (!ctx) return MONTE_EINVAL;
-  MONTE_TRY(validate(ctx, g, true));
+  MONTE_TRY(fdk_validate(ctx, g, true));
   if (!grad_vol || !grad_proj) return set_error(ctx, MONTE_EINVAL, "null gradient pointer");
   if (g->flags & MONTE_FDK_FLAT_EDGE)
     return set_error(ctx, MONTE_EUNSUPPORTED,

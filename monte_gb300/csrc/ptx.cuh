@@ -63,6 +63,34 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
   return false;
 }
 
+// try_wait that may suspend the thread for up to `hint_ns` nanoseconds
+// (PTX suspendTimeHint) while the phase is incomplete, instead of returning
+// at once: waiting warps then leave the issue slots to warps with work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t phase,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Suspend time per poll and polls of mbar_wait_sleep: at most
+// kSleepPolls * kSleepHintNs = 0.5 s before the wait is declared failed.
+constexpr uint32_t kSleepHintNs = 100000;
+constexpr uint32_t kSleepPolls = 5000;
+
+// Wait for phase `phase`, suspending between polls; false on give-up.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t phase) {
+  for (uint32_t i = 0; i < kSleepPolls; i++)
+    if (mbar_try_wait_sleep(bar, phase, kSleepHintNs)) return true;
+  return false;
+}
+
 // Make generic-proxy shared-memory writes visible to the async proxy
 // (TMA, tensor cores).
 __device__ __forceinline__ void fence_proxy_async_smem() {

@@ -53,9 +53,10 @@ __global__ void siddon_forward_kernel(SiddonDev s, const float* __restrict__ mu,
   if (!ray_of(s, r, &view, &iu, &iv, &cell)) return;
   float o[3], d[3];
   siddon_ray(s.P, s.V, s.U, s.W, view, iu, iv, o, d);
-  float L = 0.0f;
+  double Ld = 0.0;
   siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-              [&](size_t v, float len) { L = fmaf(__ldg(mu + v), len, L); });
+              [&](size_t v, double len) { Ld = fma((double)__ldg(mu + v), len, Ld); });
+  const float L = (float)Ld;
   if (line) line[cell] = L;
   if (trans) trans[cell] = expf(-L);
 }
@@ -72,14 +73,14 @@ __global__ void siddon_backward_kernel(SiddonDev s, const float* __restrict__ mu
   siddon_ray(s.P, s.V, s.U, s.W, view, iu, iv, o, d);
   float gL = grad_line ? grad_line[cell] : 0.0f;
   if (grad_trans) {
-    float L = 0.0f;
+    double Ld = 0.0;
     siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-                [&](size_t v, float len) { L = fmaf(__ldg(mu + v), len, L); });
-    gL -= grad_trans[cell] * expf(-L);  // dT/dL = -T
+                [&](size_t v, double len) { Ld = fma((double)__ldg(mu + v), len, Ld); });
+    gL -= grad_trans[cell] * expf(-(float)Ld);  // dT/dL = -T
   }
   if (gL == 0.0f) return;
   siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-              [&](size_t v, float len) { atomicAdd(grad_mu + v, gL * len); });
+              [&](size_t v, double len) { atomicAdd(grad_mu + v, gL * (float)len); });
 }
 
 int setup(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid, int vb, int ve,
@@ -130,12 +131,12 @@ int setup(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid,
   s->g.nx = grid->nx;
   s->g.ny = grid->ny;
   s->g.nz = grid->nz;
-  s->g.x0 = (float)grid->x0;
-  s->g.y0 = (float)grid->y0;
-  s->g.z0 = (float)grid->z0;
-  s->g.dx = (float)grid->dx;
-  s->g.dy = (float)grid->dy;
-  s->g.dz = (float)grid->dz;
+  s->g.x0 = grid->x0;
+  s->g.y0 = grid->y0;
+  s->g.z0 = grid->z0;
+  s->g.dx = grid->dx;
+  s->g.dy = grid->dy;
+  s->g.dz = grid->dz;
   s->view_begin = vb;
   s->view_end = ve;
   return MONTE_OK;

@@ -17,68 +17,69 @@ namespace monte {
 
 struct SiddonGrid {
   int nx, ny, nz;
-  float x0, y0, z0;        // low corner (cm)
-  float dx, dy, dz;        // voxel pitch (cm)
+  double x0, y0, z0;       // low corner (cm)
+  double dx, dy, dz;       // voxel pitch (cm)
 };
 
 // Visit the voxels a ray o + t*d (|d| = 1, t in cm) crosses inside the
-// grid, calling f(voxel index, segment length).  Crossing parameters are
-// recomputed from integer plane indices at every step, never accumulated.
+// grid, calling f(voxel index, segment length in cm, as a double).
+// Crossing parameters are recomputed from integer plane indices at every
+// step, never accumulated.
+//
+// The walk runs in double.  Its parameters reach the ray's length inside the
+// grid (tens of cm) while segments are a fraction of a voxel, so in float
+// every segment length would carry an absolute error of ~1 ulp(t) -- about
+// 5e-5 of a 0.8 mm segment -- and the line integral of a ray crossing a few
+// strong boundaries would drift by more than 1e-5 relative.  The ray's entry
+// point (a small difference of large numbers: the source sits hundreds of
+// voxels from the grid) is likewise computed in double.
 template <typename F>
 __device__ __forceinline__ void siddon_walk(const SiddonGrid& g, float ox, float oy, float oz,
                                             float dx, float dy, float dz, F&& f) {
-  // Per-ray set-up in double: the source sits hundreds of voxels from the
-  // grid, and in float the entry point (a small difference of large
-  // numbers) would shift the ray by ~1e-5 voxel -- enough to move the plane
-  // crossings of rays that graze a plane.  The walk itself runs in float
-  // from the entry point, where all parameters stay within the grid's extent.
-  const double invd[3] = {1.0 / (double)g.dx, 1.0 / (double)g.dy, 1.0 / (double)g.dz};
-  const double od[3] = {((double)ox - (double)g.x0) * invd[0], ((double)oy - (double)g.y0) * invd[1],
-                        ((double)oz - (double)g.z0) * invd[2]};
+  const double invd[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
+  const double od[3] = {((double)ox - g.x0) * invd[0], ((double)oy - g.y0) * invd[1],
+                        ((double)oz - g.z0) * invd[2]};
   const double dd[3] = {(double)dx * invd[0], (double)dy * invd[1], (double)dz * invd[2]};
   const int n[3] = {g.nx, g.ny, g.nz};
-  double t0d = 0.0, t1d = 1.0e300;
+  double t0 = 0.0, t1 = 1.0e300;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     if (dd[a] == 0.0) {
       if (od[a] < 0.0 || od[a] >= (double)n[a]) return;
     } else {
       double ta = -od[a] / dd[a], tb = ((double)n[a] - od[a]) / dd[a];
-      t0d = fmax(t0d, fmin(ta, tb));
-      t1d = fmin(t1d, fmax(ta, tb));
+      t0 = fmax(t0, fmin(ta, tb));
+      t1 = fmin(t1, fmax(ta, tb));
     }
   }
-  if (!(t0d < t1d)) return;
-  float e[3], dir[3];
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    e[a] = (float)(od[a] + t0d * dd[a]);
-    dir[a] = (float)dd[a];
-  }
-  float t1 = (float)(t1d - t0d);
-  // voxel at the entry: evaluate 1e-4 voxel inside the grid
+  if (!(t0 < t1)) return;
+  // voxel at the entry: evaluate 1e-4 voxel inside the grid; crossing of
+  // plane p along axis a at t = p * inv[a] + c[a]
   int idx[3], step[3];
-  float tnext[3];
-  const float dmax = fmaxf(fabsf(dir[0]), fmaxf(fabsf(dir[1]), fabsf(dir[2])));
-  const float tm = 1e-4f / dmax;
+  double tnext[3], inv[3], c[3];
+  const double dmax = fmax(fabs(dd[0]), fmax(fabs(dd[1]), fabs(dd[2])));
+  const double tm = t0 + 1e-4 / dmax;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    float p = fmaf(tm, dir[a], e[a]);
-    int i = (int)floorf(p);
+    const double p = od[a] + tm * dd[a];
+    const int i = (int)floor(p);
     idx[a] = min(max(i, 0), n[a] - 1);
-    step[a] = dir[a] > 0.0f ? 1 : -1;
-    if (dir[a] == 0.0f) {
-      tnext[a] = 3.0e38f;
+    step[a] = dd[a] > 0.0 ? 1 : -1;
+    if (dd[a] == 0.0) {
+      inv[a] = 0.0;
+      c[a] = 0.0;
+      tnext[a] = 1.0e300;
     } else {
-      float plane = (float)(idx[a] + (step[a] > 0 ? 1 : 0));
-      tnext[a] = (plane - e[a]) / dir[a];
+      inv[a] = 1.0 / dd[a];
+      c[a] = -od[a] * inv[a];
+      tnext[a] = fma((double)(idx[a] + (step[a] > 0 ? 1 : 0)), inv[a], c[a]);
     }
   }
-  float t = 0.0f;
+  double t = t0;
   const int max_steps = g.nx + g.ny + g.nz + 3;
   for (int it = 0; it < max_steps && t < t1; it++) {
     int a = (tnext[0] <= tnext[1]) ? ((tnext[0] <= tnext[2]) ? 0 : 2) : ((tnext[1] <= tnext[2]) ? 1 : 2);
-    float tn = fminf(tnext[a], t1);
+    double tn = fmin(tnext[a], t1);
     if (tn > t) {
       size_t v = ((size_t)idx[2] * g.ny + idx[1]) * g.nx + idx[0];
       f(v, tn - t);
@@ -86,8 +87,7 @@ __device__ __forceinline__ void siddon_walk(const SiddonGrid& g, float ox, float
     t = tn;
     idx[a] += step[a];
     if (idx[a] < 0 || idx[a] >= n[a]) break;
-    float plane = (float)(idx[a] + (step[a] > 0 ? 1 : 0));
-    tnext[a] = (plane - e[a]) / dir[a];
+    tnext[a] = fma((double)(idx[a] + (step[a] > 0 ? 1 : 0)), inv[a], c[a]);
   }
 }
 

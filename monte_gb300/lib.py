@@ -70,6 +70,12 @@ def load(build_if_missing=False):
                                  C.POINTER(abi.McStats), C.c_int]
     lib.monte_mc_finalize.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P, P, P,
                                       P, P, P, C.c_int]
+    lib.monte_batch_create.argtypes = [P, C.POINTER(abi.McXcom), C.POINTER(abi.BatchJob),
+                                       C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+    lib.monte_batch_run.argtypes = [P]
+    lib.monte_batch_stats.argtypes = [P, C.POINTER(abi.McStats)]
+    lib.monte_batch_bp_variant.argtypes = [P, C.c_int]
+    lib.monte_batch_destroy.argtypes = [P]
     SG = C.POINTER(abi.SiddonGrid)
     lib.monte_siddon_forward.argtypes = [P, MG, SG, P, C.c_int, C.c_int, P, P, C.c_int]
     lib.monte_siddon_backward.argtypes = [P, MG, SG, P, C.c_int, C.c_int, P, P, P, C.c_int]
@@ -233,3 +239,47 @@ class Context:
         self.check(self.lib.monte_fdk(self.h, C.byref(g), _ptr(proj)[0], _ptr(filtered)[0],
                                       _ptr(vol_xy)[0], _ptr(vol_zy)[0], filter_mode, bp_mode,
                                       mem))
+
+    # ---- batches ---------------------------------------------------------
+    def batch(self, xcom, jobs, mode=abi.MONTE_BATCH_FUSED, options=0):
+        """monte_batch_create over a list of abi.BatchJob; returns a Batch."""
+        arr = (abi.BatchJob * len(jobs))(*jobs)
+        h = C.c_void_p()
+        self.check(self.lib.monte_batch_create(self.h, C.byref(xcom), arr, len(jobs), mode,
+                                               options, C.byref(h)))
+        return Batch(self, h)
+
+
+class Batch:
+    """A created batch plan (monte_batch_*); destroyed with close()."""
+
+    def __init__(self, ctx, handle):
+        self.ctx, self.h = ctx, handle
+
+    def run(self):
+        self.ctx.check(self.ctx.lib.monte_batch_run(self.h))
+
+    def stats(self):
+        st = abi.McStats()
+        self.ctx.check(self.ctx.lib.monte_batch_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def bp_variant(self, job):
+        return self.ctx.lib.monte_batch_bp_variant(self.h, job)
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.monte_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -10,6 +10,7 @@ import oracle
 from helpers import golden, past_end_voxels, rel_rms
 from inputs import fdk_projections
 from monte_gb300 import abi
+from monte_gb300.lib import MonteError
 
 pytestmark = pytest.mark.gpu
 
@@ -158,3 +159,17 @@ def test_autotune_picks_a_tile_and_all_tiles_agree(ctx):
     _, got = _run(ctx, g, proj, bp_mode=abi.MONTE_BP_TILED)
     assert ctx.last_bp_variant() == best
     assert rel_rms(got, ref) < 2e-6
+    # every tile shape (pipeline depth, register budget, block shape)
+    v = 0
+    while True:
+        try:
+            ctx.set_bp_variant(v)
+        except MonteError:
+            break
+        _, got = _run(ctx, g, proj, bp_mode=abi.MONTE_BP_TILED)
+        ctx.check_status()
+        assert ctx.last_bp_variant() == v
+        assert rel_rms(got, ref) < 2e-6, v
+        v += 1
+    assert v >= 12
+    ctx.set_bp_variant(best)
