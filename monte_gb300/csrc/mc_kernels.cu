@@ -40,11 +40,23 @@ __device__ __forceinline__ void decompose(const McDev& d, unsigned long long h, 
   const unsigned long long per = d.P.per;
   const unsigned nv_roi = (unsigned)(d.P.v_end - d.P.v_begin);
   const unsigned nu_roi = (unsigned)(d.P.u_end - d.P.u_begin);
-  unsigned long long rest = h / per;
-  *k = h - rest * per;
-  unsigned long long npix = (unsigned long long)nu_roi * nv_roi;
-  unsigned long long vw = rest / npix;
-  unsigned pix = (unsigned)(rest - vw * npix);
+  const unsigned long long npix = (unsigned long long)nu_roi * nv_roi;
+  unsigned long long vw;
+  unsigned pix;
+  if ((h >> 32) == 0 && (per >> 32) == 0 && (npix >> 32) == 0) {
+    // 32-bit divisions (a 64-bit one is a long software routine); the
+    // same quotients
+    const unsigned h32 = (unsigned)h, per32 = (unsigned)per, np32 = (unsigned)npix;
+    const unsigned r32 = h32 / per32;
+    *k = h32 - r32 * per32;
+    vw = r32 / np32;
+    pix = r32 - (unsigned)vw * np32;
+  } else {
+    const unsigned long long rest = h / per;
+    *k = h - rest * per;
+    vw = rest / npix;
+    pix = (unsigned)(rest - vw * npix);
+  }
   *view = d.P.view_begin + (int)vw;
   *iu = d.P.u_begin + (int)(pix / nv_roi);
   *iv = d.P.v_begin + (int)(pix % nv_roi);
@@ -85,7 +97,7 @@ __global__ void __launch_bounds__(128) mc_plain_kernel(McDev d) {
             long long cell = mc_detector_index(&d.P, d.V, &p);
             if (kind >= 0 && cell >= 0) {
               atomicAdd(kind == 0 ? &d.prim[cell] : &d.scat[cell], 1ull);
-              st[3 + kind]++;
+              if (kind == 0) st[3]++; else st[4]++;  // no run-time index: st stays in registers
             }
             break;
           } else {
@@ -99,7 +111,11 @@ __global__ void __launch_bounds__(128) mc_plain_kernel(McDev d) {
   warp_stats(d, st);
 }
 
-__global__ void __launch_bounds__(256) mc_persistent_kernel(McDev d) {
+// 64 registers: four CTAs (32 warps) per SM; measured against 80 registers
+// (three CTAs) and a four-step flight with the label reads issued together,
+// this form has the highest throughput: the kernel is bound by issue, not by
+// the latency of the label gathers
+__global__ void __launch_bounds__(256, 4) mc_persistent_kernel(McDev d) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -167,7 +183,7 @@ __global__ void __launch_bounds__(256) mc_persistent_kernel(McDev d) {
       if (lane == __ffs(grp) - 1) {
         atomicAdd(kind == 0 ? &d.prim[cell] : &d.scat[cell], (unsigned long long)__popc(grp));
       }
-      st[3 + kind]++;
+      if (kind == 0) st[3]++; else st[4]++;  // no run-time index: st stays in registers
     }
     // ---- real collisions, processed as a batch ---------------------------
     const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
@@ -185,7 +201,7 @@ __global__ void __launch_bounds__(256) mc_persistent_kernel(McDev d) {
 // concatenated history ranges, and a lane that takes history h finds its
 // job by binary search over the range starts.  Everything else is the
 // single-job kernel's loop, reading the job's parameters through a pointer.
-__global__ void __launch_bounds__(256) mc_persistent_batch_kernel(
+__global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
     const McDev* __restrict__ jobs, const unsigned long long* __restrict__ starts, int n_jobs,
     unsigned long long total, unsigned long long* counter, unsigned long long* stats) {
   const unsigned FULL = 0xffffffffu;
@@ -262,7 +278,7 @@ __global__ void __launch_bounds__(256) mc_persistent_batch_kernel(
     if (dst) {
       const unsigned grp = __match_any_sync(tal, (unsigned long long)dst);
       if (lane == __ffs(grp) - 1) atomicAdd(dst, (unsigned long long)__popc(grp));
-      st[3 + kind]++;
+      if (kind == 0) st[3]++; else st[4]++;  // no run-time index: st stays in registers
     }
     const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
     const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);

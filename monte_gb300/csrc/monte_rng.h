@@ -95,7 +95,9 @@ MONTE_HD uint32_t monte_stream_u32(monte_stream* s) {
     s->buf[3] = r.v[3];
   }
   s->next++;
-  return s->buf[w];
+  /* a select, not buf[w]: a run-time index would keep the buffer (and the
+   * photon around it) in local memory */
+  return w == 0 ? s->buf[0] : w == 1 ? s->buf[1] : w == 2 ? s->buf[2] : s->buf[3];
 }
 
 /* Uniform on (0, 1] with 24-bit resolution, like curand_uniform's range

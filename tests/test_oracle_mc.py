@@ -98,3 +98,4 @@ def test_compton_sampler_is_klein_nishina(E):
     expect = n * np.diff(np.interp(edges, fine, cdf))
     x2 = float(np.sum((h - expect) ** 2 / expect))
     assert chi2.sf(x2, len(h) - 1) > 1e-3, x2
+
