@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form FDK timing")
     ap.add_argument("--no-mc", action="store_true", help="skip the Monte Carlo timing")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-scan timing")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-mode timing")
     ap.add_argument("--batch-scale", type=float, default=0.1,
                     help="histories per view of the batched scans, as a fraction of 1e6-1e7")
     ap.add_argument("--tile", type=int, default=-1,
@@ -53,6 +54,8 @@ def parse():
 
 
 WORKLOAD = "fdk: 360 views x 512(u) x 384(v) FP32 @0.8mm, SOD 500, SDD 1000 mm -> 325^3 FP32 @0.4mm"
+# measured DRAM traffic per backprojection launch of WORKLOAD, by tile shape
+BP_TRAFFIC = {24: 331.70e6 + 142.00e6, 16: 904.65e6 + 164.43e6}
 
 
 def geometry(small=False):
@@ -302,6 +305,81 @@ def batch_bench(ctx, device, scale):
     return out
 
 
+DIFF_WORKLOAD = ("differentiable mode: 257^3 FP32 at 0.8 mm, 360 views x 512 x 384 at 0.8 mm, "
+                 "SOD 500, SDD 1000 mm; x, p, x* seeded ellipsoid data")
+
+
+def diff_bench(ctx, device):
+    """Wall time of the gradients of the differentiable mode at 257^3:
+    ||A x - p||^2 w.r.t. x (forward projector A, then its adjoint, the
+    backprojector), ||FDK(p) - x*||^2 w.r.t. p (FDK, then monte_fdk_backward)
+    and exp(-integral mu) w.r.t. mu (Siddon forward and adjoint).  One
+    warm-up and two timed calls each; CUDA events on the context's stream."""
+    import torch
+    from monte_gb300 import abi, phantoms
+    g = abi.fdk_geom_recon325(n_views=360, nu=512, nv=384, pitch_mm=0.8, n=257, voxel_mm=0.8)
+    g.flags = 0  # the textbook operator (the adjoints need no flat-edge wrap)
+    stream = torch.cuda.current_stream(device)
+    ell = phantoms.random_ellipsoids(1005)
+    p = phantoms.ellipsoid_line_integrals(g, ell, 0.01, 5, device=device).contiguous()
+    ax = (torch.arange(g.nx, device=device, dtype=torch.float64) - g.nx / 2 + 0.5) * g.dvox
+    Z, Y, X = torch.meshgrid(ax, ax, ax, indexing="ij")
+    x = phantoms.ellipsoid_density(ell, X, Y, Z).float().contiguous()
+    xstar = phantoms.ellipsoid_density(phantoms.random_ellipsoids(1006), X, Y, Z).float().contiguous()
+    del X, Y, Z
+    proj_fs = torch.empty((g.n_views, g.nv, g.nu), device=device)
+    vol = torch.empty_like(x)
+    gp = torch.empty_like(p)
+
+    def timed(fn, reps=2):
+        fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    updates = g.nx * g.ny * g.nz * g.n_views
+    # ||A x - p||^2: A x in filtered-space layout [view][v][u]; p transposed alike
+    p_vu = p.transpose(1, 2).contiguous()
+
+    def grad_x():
+        ctx.fdk_forward_project(g, x, proj_fs)
+        proj_fs.sub_(p_vu).mul_(2.0)
+        ctx.fdk_backproject(g, proj_fs, vol, mode=abi.MONTE_BP_TILED)
+
+    t_fp = timed(lambda: ctx.fdk_forward_project(g, x, proj_fs))
+    t_gx = timed(grad_x)
+
+    def grad_p():
+        ctx.fdk(g, p, vol, filter_mode=abi.MONTE_FILTER_BF16X3, bp_mode=abi.MONTE_BP_TILED)
+        vol.sub_(xstar).mul_(2.0)
+        ctx.fdk_backward(g, vol, gp)
+
+    t_gp = timed(grad_p)
+    # primary signal: the Monte Carlo's rays through mu = x (1/cm)
+    mg = abi.mc_geom(360, 512, 384, 0.08, 50.0, 100.0, 20.0)
+    grid = abi.siddon_grid((g.nz, g.ny, g.nx), g.dvox, (-g.nx * g.dvox / 2,) * 3)
+    tr = torch.empty((mg.n_views, mg.nu, mg.nv), device=device)
+    gmu = torch.zeros_like(x)
+    gt = torch.ones_like(tr)
+    t_sf = timed(lambda: ctx.siddon_forward(mg, grid, x, (0, mg.n_views), transmission=tr), reps=1)
+    t_sb = timed(lambda: ctx.siddon_backward(mg, grid, x, (0, mg.n_views), gmu,
+                                             grad_transmission=gt), reps=1)
+    ctx.check_status()
+    rays = mg.n_views * mg.nu * mg.nv
+    return {"workload": DIFF_WORKLOAD,
+            "forward_projector": {"ms": t_fp * 1e3, "gups": updates / t_fp / 1e9},
+            "grad_x_least_squares": {"ms": t_gx * 1e3, "note": "A x - p, then 2 A^T r (tiled)"},
+            "grad_p_fdk": {"ms": t_gp * 1e3, "note": "FDK (BF16x3 + tiled), then FDK^T"},
+            "siddon_forward": {"ms": t_sf * 1e3, "rays_per_s": rays / t_sf},
+            "siddon_backward": {"ms": t_sb * 1e3, "rays_per_s": rays / t_sb}}
+
+
 def run_reference(args):
     world, rank, local = dist_setup(args)
     if rank != 0:
@@ -418,13 +496,10 @@ def run_ours(args):
     bp_flops = 10.0 * updates
     bp_bytes = g.n_views * g.nu * g.nv * 4 + g.nx * g.ny * g.nz * 4
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    prof = {}
-    try:
-        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
-            prof = json.load(f)
-    except OSError:
-        pass
-    traffic = prof.get("bp_tiled" if bmode == abi.MONTE_BP_TILED else "bp_plain")
+    # DRAM bytes (read + write) of one backprojection launch of this workload,
+    # from ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) for the
+    # tile shapes that lead it; profiles/bp_warp_recon325.md gives the command
+    traffic = BP_TRAFFIC.get(ctx.last_bp_variant()) if not args.small else None
 
     line = {
         "metric": "FDK GUPS (voxel-view updates/s)", "value": value, "unit": "GUPS",
@@ -477,6 +552,8 @@ def run_ours(args):
         line["gpu_launches_mc"] = 2 * 4
     if not args.no_batch and not args.small:
         line["batch"] = batch_bench(ctx, dev, args.batch_scale)
+    if not args.no_diff and not args.small:
+        line["diff"] = diff_bench(ctx, dev)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g)
     if rank == 0:

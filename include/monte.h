@@ -383,9 +383,10 @@ typedef struct monte_batch_job {
                                     Carlo kernel, finalize, FP32 filter, plain
                                     backprojection (no graph) */
 /* monte_batch_create option bits. */
-#define MONTE_BATCH_AUTOTUNE 0x1 /* time the tile shapes of the tiled
+#define MONTE_BATCH_AUTOTUNE 0x1 /* time the leading tile shapes of the tiled
                                     backprojector on every distinct FDK
-                                    geometry at creation (FUSED only) */
+                                    geometry at creation (FUSED only); the
+                                    full sweep is monte_fdk_autotune */
 
 typedef struct monte_batch monte_batch;
 

@@ -326,7 +326,8 @@ int create_plan(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* j
         }
       if (!found) {
         MONTE_CUDA(ctx, cudaMemsetAsync(b.filtered, 0, b.ncell * 4, ctx->stream));
-        MONTE_TRY(fdk_tune_bp(ctx, &b.job.fdk, b.bpv, b.bpvd, b.filtered, b.job.vol_xy, &v));
+        MONTE_TRY(fdk_tune_bp(ctx, &b.job.fdk, b.bpv, b.bpvd, b.filtered, b.job.vol_xy, &v,
+                              kBpQuickCandidates, kBpQuickCandidatesN, 2));
         tuned.push_back({key, v});
       }
     } else {

@@ -71,11 +71,16 @@ struct FdkHostTables {
 void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t);
 // Argument checks of the FDK entry points (sets the context's error text).
 int fdk_validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid);
-// Time every tiled backprojector shape that fits g (three launches each on
-// the context's stream, the first discarded) into scratch `dv` from
-// filtered projections `df`; *best = fastest shape, -1 if none fits.
+// Time tiled backprojector shapes that fit g (`reps` launches each on the
+// context's stream, the first discarded) into scratch `dv` from filtered
+// projections `df`; *best = fastest shape, -1 if none fits.  candidates:
+// the shapes to time (NULL: all of them).
 int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
-                const BpViewD* viewsd, const float* df, float* dv, int* best);
+                const BpViewD* viewsd, const float* df, float* dv, int* best,
+                const int* candidates, int n_candidates, int reps);
+// Shapes that led on the reference-size workloads, for quick tuning.
+extern const int kBpQuickCandidates[];
+extern const int kBpQuickCandidatesN;
 
 // Kernel launchers (return cudaGetLastError()).
 cudaError_t launch_fdk_filter_fp32(const FdkDev& d, const float* proj, const float* weights,

@@ -150,17 +150,21 @@ void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t) {
 }
 
 int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
-                const BpViewD* viewsd, const float* df, float* dv, int* best) {
+                const BpViewD* viewsd, const float* df, float* dv, int* best,
+                const int* candidates, int n_candidates, int reps) {
   FdkDev d = make_fdk_dev(*g);
+  if (reps < 2) reps = 2;
   cudaEvent_t e0, e1;
   MONTE_CUDA(ctx, cudaEventCreate(&e0));
   MONTE_CUDA(ctx, cudaEventCreate(&e1));
   int pick = -1;
   float best_ms = 3.0e38f;
-  for (int v = 0; v < fdk_bp_tiled_variants(); v++) {
+  const int n = candidates ? n_candidates : fdk_bp_tiled_variants();
+  for (int i = 0; i < n; i++) {
+    const int v = candidates ? candidates[i] : i;
     if (!fdk_bp_tiled_supported(d, v)) continue;
     float ms_min = 3.0e38f;
-    for (int rep = 0; rep < 3; rep++) {
+    for (int rep = 0; rep < reps; rep++) {
       cudaEventRecord(e0, ctx->stream);
       cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, dv, nullptr, v, ctx->d_status,
                                           ctx->stream);
@@ -424,7 +428,7 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
   const BpView* views = (const BpView*)ctx->fdk_views.ptr;
   const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
   int pick = -1;
-  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick));
+  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick, nullptr, 0, 3));
   ctx->bp_tune_choice = pick;
   if (best) *best = pick;
   return monte_ctx_check_status(ctx);
