@@ -179,6 +179,47 @@ int monte_fdk_last_bp_variant(const monte_ctx* ctx);
 int monte_ctx_check_status(monte_ctx* ctx);
 
 /* ======================================================================
+ *  2-D fan-beam FBP
+ * ====================================================================== */
+
+/*
+ * Geometry of the reference's 2-D fan-beam FBP, recon/fbp2.cpp: n_det
+ * detector elements at `pitch` (element c at u = -half + pitch*c, the
+ * weighting's convention, :36-40), views k*360/n_views degrees, of which
+ * [view_begin, view_end) are backprojected (the reference skips view 0,
+ * :89); pixel (s, t) of the nx x ny image at X = x0 + pix*s, Y = y0 - pix*t;
+ * the nearest detector element int((half - u') / pitch) is read (no
+ * interpolation, :120-126); output image[t][s] += (D^2/(D-d)^2) * q * dbeta
+ * * scale (:148).  Flag MONTE_FDK_TAN_DEGREES: tan() of the view angle in
+ * degrees (as the reference evaluates it, :135).
+ */
+typedef struct monte_fbp2_geom {
+  int32_t n_views, n_det;
+  int32_t view_begin, view_end;
+  int32_t nx, ny;
+  int32_t flags;              /* MONTE_FDK_TAN_DEGREES */
+  int32_t reserved0;
+  double pitch, half;         /* detector pitch and half extent (cm) */
+  double sod, sdd;            /* source to axis, source to detector (cm) */
+  double wdist;               /* D of the weights */
+  double pix, x0, y0;         /* image pitch and origin (cm) */
+  double scale;
+} monte_fbp2_geom;
+
+/* Defaults equal to recon/fbp2.cpp: 65 elements of 0.5 cm, 360 views of
+ * which 1..359 are backprojected, SOD 160, SDD 220, D 60, 256^2 image at
+ * 0.1 cm from (-12.8, 12.8), scale 1.7, tan of degrees. */
+void monte_fbp2_geom_reference(monte_fbp2_geom* g);
+
+/* Weighting + ramp filter + backprojection: proj[view][det] ->
+ * filtered[view][det] (may be NULL) and image[ny][nx] (overwritten).
+ * recon/fbp2.cpp:15-152.  Double arithmetic as the reference's; the
+ * filtered array and the image are float as there.  The call waits for the
+ * context's stream (its per-view tables are staged from the host). */
+int monte_fbp2(monte_ctx* ctx, const monte_fbp2_geom* g, const float* proj, float* filtered,
+               float* image, int mem);
+
+/* ======================================================================
  *  Monte Carlo
  * ====================================================================== */
 

@@ -97,6 +97,37 @@ def fdk_geom_reference325():
 MONTE_MC_STALE_SIN_PHI = 0x1
 MONTE_MC_FIRST_COMPTON_Z = 0x2
 MONTE_MC_NO_RAYLEIGH_TALLY = 0x4
+class Fbp2Geom(C.Structure):
+    """monte_fbp2_geom."""
+
+    _fields_ = [
+        ("n_views", C.c_int32), ("n_det", C.c_int32),
+        ("view_begin", C.c_int32), ("view_end", C.c_int32),
+        ("nx", C.c_int32), ("ny", C.c_int32),
+        ("flags", C.c_int32), ("reserved0", C.c_int32),
+        ("pitch", C.c_double), ("half", C.c_double),
+        ("sod", C.c_double), ("sdd", C.c_double), ("wdist", C.c_double),
+        ("pix", C.c_double), ("x0", C.c_double), ("y0", C.c_double),
+        ("scale", C.c_double),
+    ]
+
+
+def fbp2_geom_reference():
+    """recon/fbp2.cpp: 65 elements of 0.5 cm (half 16.25), 360 views of which
+    1..359 are backprojected, SOD 160, SDD 220, D 60, 256^2 image at 0.1 cm
+    from (-12.8, 12.8), scale 1.7, tan of degrees."""
+    g = Fbp2Geom()
+    g.n_views, g.n_det = 360, 65
+    g.view_begin, g.view_end = 1, 360
+    g.nx = g.ny = 256
+    g.flags = MONTE_FDK_TAN_DEGREES
+    g.pitch, g.half = 0.5, 16.25
+    g.sod, g.sdd, g.wdist = 160.0, 220.0, 60.0
+    g.pix, g.x0, g.y0 = 0.1, -12.8, 12.8
+    g.scale = 1.7
+    return g
+
+
 MONTE_MC_PLAIN = 0
 MONTE_MC_PERSISTENT = 1
 

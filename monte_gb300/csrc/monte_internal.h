@@ -65,6 +65,7 @@ enum ScratchSlot {
   kScratchAux2 = 9,
   kScratchAux3 = 10,
   kScratchStats = 11,
+  kScratchFbp2 = 12,
 };
 
 int set_error(monte_ctx* ctx, int code, const char* fmt, ...);

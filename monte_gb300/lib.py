@@ -76,6 +76,10 @@ def load(build_if_missing=False):
     lib.monte_batch_stats.argtypes = [P, C.POINTER(abi.McStats)]
     lib.monte_batch_bp_variant.argtypes = [P, C.c_int]
     lib.monte_batch_destroy.argtypes = [P]
+    F2 = C.POINTER(abi.Fbp2Geom)
+    lib.monte_fbp2_geom_reference.argtypes = [F2]
+    lib.monte_fbp2_geom_reference.restype = None
+    lib.monte_fbp2.argtypes = [P, F2, P, P, P, C.c_int]
     SG = C.POINTER(abi.SiddonGrid)
     lib.monte_siddon_forward.argtypes = [P, MG, SG, P, C.c_int, C.c_int, P, P, C.c_int]
     lib.monte_siddon_backward.argtypes = [P, MG, SG, P, C.c_int, C.c_int, P, P, P, C.c_int]
@@ -239,6 +243,13 @@ class Context:
         self.check(self.lib.monte_fdk(self.h, C.byref(g), _ptr(proj)[0], _ptr(filtered)[0],
                                       _ptr(vol_xy)[0], _ptr(vol_zy)[0], filter_mode, bp_mode,
                                       mem))
+
+    # ---- 2-D fan-beam FBP --------------------------------------------------
+    def fbp2(self, g, proj, image, filtered=None):
+        """monte_fbp2: proj[view][det] -> image[ny][nx] (and filtered[view][det])."""
+        mem = _mem_of(proj, image, filtered)
+        self.check(self.lib.monte_fbp2(self.h, C.byref(g), _ptr(proj)[0], _ptr(filtered)[0],
+                                       _ptr(image)[0], mem))
 
     # ---- batches ---------------------------------------------------------
     def batch(self, xcom, jobs, mode=abi.MONTE_BATCH_FUSED, options=0):

@@ -131,6 +131,31 @@ def cylinder_inserts_labels(seed=1001, n=65, voxel_mm=1.0, radius_mm=28.0, inser
     return lab, voxel_mm / 10.0, (-h, -h, -h)
 
 
+# densities (g/cm^3) of the analytic phantom of monte_cu/CBCT_real325.cu:122-123
+CA_ROD_DENSITY = (1.0, 1.55)
+
+
+def ca_rod_labels(voxel_cm=0.1):
+    """Voxelised form of the analytic phantom that monte_cu/CBCT_real325.cu
+    tests in its Woodcock loop (:916-928): a water cylinder of radius 10 cm
+    along x, |x| <= 10 cm, holding eight Ca rods of radius 1.5 cm whose axes
+    sit 5 cm from the cylinder's, every 45 degrees in the y-z plane; air
+    outside.  A voxel takes the label of its centre: 0 air, 1 water, 2 Ca
+    (materials [-1, 0, 1] with densities [0, 1.0, 1.55]).  Covers the box
+    [-10, 10]^3 cm.  Returns (labels[z][y][x] uint8, voxel cm, origin cm,
+    densities, materials)."""
+    n = int(round(20.0 / voxel_cm))
+    ax = (np.arange(n) + 0.5) * voxel_cm - 10.0
+    Z, Y, X = np.meshgrid(ax, ax, ax, indexing="ij")
+    lab = np.zeros((n, n, n), np.uint8)
+    lab[(Y * Y + Z * Z <= 100.0) & (np.abs(X) <= 10.0)] = 1
+    for k in range(8):
+        a = k * np.pi / 4.0
+        cy, cz = 5.0 * np.sin(a), 5.0 * np.cos(a)
+        lab[((Y - cy) ** 2 + (Z - cz) ** 2 <= 1.5 ** 2) & (lab == 1)] = 2
+    return lab, voxel_cm, (-10.0, -10.0, -10.0), [0.0, *CA_ROD_DENSITY], [-1, 0, 1]
+
+
 def ellipsoid_labels(seed=1003, n=325, voxel_mm=0.8, n_ell=20):
     """The 325^3 phantom of the full Monte Carlo workload: 20 seeded
     ellipsoids (centres U(-80,80) mm, semi-axes U(10,70) mm, random

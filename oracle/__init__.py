@@ -53,7 +53,20 @@ def lib():
         _LIB.oracle_siddon_forward.argtypes = [C.POINTER(abi.McGeom), sg, f, C.c_int, C.c_int, d]
         _LIB.oracle_siddon_backward.argtypes = [C.POINTER(abi.McGeom), sg, f, C.c_int, C.c_int,
                                                 d, d, d]
+        _LIB.oracle_fbp2.argtypes = [C.POINTER(abi.Fbp2Geom), f, f, f]
+        _LIB.oracle_fbp2.restype = None
     return _LIB
+
+
+def fbp2(g, proj):
+    """recon/fbp2.cpp restated: proj[view][det] float32 -> (filtered
+    [view][det], image[ny][nx]) float32."""
+    proj = np.ascontiguousarray(proj, np.float32)
+    assert proj.shape == (g.n_views, g.n_det)
+    filt = np.zeros_like(proj)
+    img = np.zeros((g.ny, g.nx), np.float32)
+    lib().oracle_fbp2(C.byref(g), _fp(proj), _fp(filt), _fp(img))
+    return filt, img
 
 
 def siddon_forward(g, grid, mu, views):

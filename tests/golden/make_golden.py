@@ -10,6 +10,8 @@ tests/golden/inputs.py):
                 xy slab [256][256][125:130], 4 filtered views
   fdk325.npz    recon/bp3d20_325.cpp on fdk_projections(360,325,325,seed=1325):
                 xy slab, filtered rows of 4 views
+  fbp2.npz      recon/fbp2.cpp on fdk_projections(360,65,1,seed=2065):
+                its filtered projections and 256x256 image
   cbct_real2.npz  monte_cpp/CBCT_real2.cpp (10^7 histories from pixel
                 (32,32) at 140 keV through the spher01.raw water sphere):
                 the 65x65 Compton-scatter tally it writes
@@ -64,6 +66,18 @@ def fdk(name, n, seed, binary, in_name, out_stem, view_ids, row_ids):
     print(name, "xy slab norm", float(np.linalg.norm(out["xy_slab"])))
 
 
+def fbp2():
+    proj = fdk_projections(360, 65, 1, 2065).reshape(360, 65)
+    with tempfile.TemporaryDirectory() as tmp:
+        proj.tofile(os.path.join(tmp, "map5_20_2e5.raw"))
+        run("fbp2", tmp)
+        filt = np.fromfile(os.path.join(tmp, "projection_test\\outproj2e5.raw"), np.float32)
+        img = np.fromfile(os.path.join(tmp, "projection_test\\testxyo2e5.raw"), np.float32)
+    np.savez(os.path.join(HERE, "fbp2.npz"), seed=np.int64(2065), filtered=filt.reshape(360, 65),
+             image=img.reshape(256, 256))
+    print("fbp2 image norm", float(np.linalg.norm(img)))
+
+
 def parse_xcom(path):
     """BOM/CRLF-tolerant parse of an XCOM csv: row r (1-based) -> index r
     (monte_cpp/CBCT_real2.cpp:633-668); index 0 repeats row 1."""
@@ -115,6 +129,7 @@ def main():
                              "2mh20kyu2", [0, 97, 201, 359], []),
         "fdk325": lambda: fdk("fdk325", 325, 1325, "bp3d20_325", "mapg325_0_2tca.raw",
                               "ca0_2t", [0, 97, 201, 359], [0, 100, 162, 324]),
+        "fbp2": fbp2,
         "cbct_real2": cbct_real2,
     }
     for k, fn in jobs.items():

@@ -55,3 +55,15 @@ def test_monte_mc_program_writes_reference_files(tmp_path):
     assert np.array_equal(m0, want)
     # the field outside the cylinder shadow is unattenuated: all histories reach it
     assert np.median(p0.reshape(views, 325, 325)[:, :5, :]) == per
+
+
+def test_monte_fbp2_program_matches_fbp2(tmp_path):
+    gold = golden("fbp2")
+    proj = fdk_projections(360, 65, 1, int(gold["seed"])).reshape(360, 65)
+    proj.tofile(tmp_path / "map5_20_2e5.raw")
+    subprocess.run([os.path.join(PROG, "monte_fbp2")], cwd=tmp_path, check=True,
+                   capture_output=True)
+    img = np.fromfile(tmp_path / "projection_test\\testxyo2e5.raw", np.float32).reshape(256, 256)
+    filt = np.fromfile(tmp_path / "projection_test\\outproj2e5.raw", np.float32).reshape(360, 65)
+    assert np.array_equal(img, gold["image"])
+    assert np.array_equal(filt, gold["filtered"])
