@@ -102,10 +102,12 @@ cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpVi
                                 const float* filtered, float* vol_xy, float* vol_zy,
                                 int variant, int* status, cudaStream_t st);
 // Adjoints (fdk_adjoint.cu): forward projector = transpose of the plain
-// backprojector, into filtered-space layout [view][v][u]; adjoint of the
-// weighting + filter, [view][v][u] -> [view][u][v].
+// backprojector, into filtered-space layout [view][v][u] (vol_z: scratch of
+// the volume's size for its z-major copy); adjoint of the weighting +
+// filter, [view][v][u] -> [view][u][v].
 cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
-                                       const float* vol, float* out, cudaStream_t st);
+                                       const float* vol, float* vol_z, float* out,
+                                       cudaStream_t st);
 cudaError_t launch_fdk_filter_adjoint(const FdkDev& d, const float* g, const float* weights,
                                       const float* taps_half, float* h, cudaStream_t st);
 int fdk_bp_tiled_variants();
@@ -186,21 +188,6 @@ __device__ __forceinline__ bool bp_ref_voxel(const FdkDev& d, const BpViewD& v, 
   return true;
 }
 
-// Whether a float-path evaluation is close enough to a discontinuity of the
-// reference operator that it must be re-decided in double.
-__device__ __forceinline__ bool bp_near_edge(const FdkDev& d, float ts, float up, float vp, float x,
-                                             float y) {
-  return fabsf(ts) < 1e-4f || fabsf(fabsf(up) - d.half_u) < 1e-4f * d.half_u ||
-         fabsf(fabsf(vp) - d.half_v) < 1e-4f * d.half_v || fabsf(x - d.xmax) < 1e-3f ||
-         fabsf(y - d.ymax) < 1e-3f || fabsf(x) < 1e-3f || fabsf(y) < 1e-3f;
-}
-
-// Coefficients of one voxel-view pair of the backprojection operator:
-// vol[s,t,z] += w * factor * bilinear(F_k; xi + fx, yi + fy).  Returns false
-// when the pair contributes nothing (rejected by recon/bp3d20.cpp:116, or
-// outside the interpolation guard of :152).  The plain backprojector and
-// its adjoint (the forward projector) both use this function, so the two
-// are exact transposes of each other.
 // Voxel (X, Y) in the frame of view v: Vx along the central ray from the
 // source, Vy across it.  The reference forms (X - px) c + (Y - py) s and
 // (Y - py) c - (X - px) s in double (recon/bp3d20.cpp:103-110); with the
@@ -214,28 +201,61 @@ __device__ __forceinline__ void bp_view_frame(const FdkDev& d, const BpView& v, 
   *Vy = fmaf(Y, v.c, -(X * v.s));
 }
 
-__device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const BpViewD& vd, int s,
-                                        int t, int z, float X, float Y, float Z, int* xi, int* yi,
-                                        float* fx, float* fy, float* w) {
+// The part of bp_coef that depends only on the voxel column (X, Y) and the
+// view: computed once per column by loops that walk a column along z.
+struct BpColumn {
+  float kk;        // sdd / Vx, the magnification
+  float up, y;     // detector u' and column coordinate
+  float ts;        // the signed in-plane term of the distance weight
+  float w;         // D^2 / (D - d)^2
+  float fy;        // column fraction
+  int yi;          // column index
+  bool near;       // ts, u' or y near a discontinuity of the operator
+  bool out;        // rejected whatever z (|u'| > half_u or y outside [0, ymax])
+};
+
+__device__ __forceinline__ void bp_column(const FdkDev& d, const BpView& v, float X, float Y,
+                                          BpColumn* c) {
   float Vx, Vy;
   bp_view_frame(d, v, X, Y, &Vx, &Vy);
-  float kk = d.sdd / Vx;
-  float up = Vy * kk, vp = Z * kk;
-  float y = bp_scale(d.half_u - up, d.inv_du, d.inv_du_lo);
+  c->kk = d.sdd / Vx;
+  c->up = Vy * c->kk;
+  c->y = bp_scale(d.half_u - c->up, d.inv_du, d.inv_du_lo);
+  c->ts = X * v.c - Y * v.s;
+  c->near = fabsf(c->ts) < 1e-4f || fabsf(fabsf(c->up) - d.half_u) < 1e-4f * d.half_u ||
+            fabsf(c->y - d.ymax) < 1e-3f || fabsf(c->y) < 1e-3f;
+  c->out = fabsf(c->up) > d.half_u || !(c->y >= 0.f && c->y <= d.ymax);
+  float tt = X * v.s + Y * v.c;
+  float dd = fabsf(c->ts - v.tanb * tt) * v.rs;
+  if (c->ts < 0.f) dd = -dd;
+  float den = d.D - dd;
+  c->w = (d.D * d.D) / (den * den);
+  c->yi = (int)c->y;
+  c->fy = c->y - (float)c->yi;
+}
+
+// Coefficients of one voxel-view pair of the backprojection operator:
+// vol[s,t,z] += w * factor * bilinear(F_k; xi + fx, yi + fy).  Returns false
+// when the pair contributes nothing (rejected by recon/bp3d20.cpp:116, or
+// outside the interpolation guard of :152).  The plain backprojector and
+// its adjoint (the forward projector) both use it (directly or as
+// bp_column + bp_coef_z, the same operations), so the two are exact
+// transposes of each other.  Pairs within a small margin of a discontinuity
+// are decided in double (bp_ref_voxel).
+__device__ __forceinline__ bool bp_coef_z(const FdkDev& d, const BpColumn& c, const BpViewD& vd,
+                                          int s, int t, int z, float Z, int* xi, int* yi,
+                                          float* fx, float* fy, float* w) {
+  float vp = Z * c.kk;
   float x = bp_scale(d.half_v - vp, d.inv_dv, d.inv_dv_lo);
-  float ts = X * v.c - Y * v.s;
-  if (!bp_near_edge(d, ts, up, vp, x, y)) {
-    if (fabsf(up) > d.half_u || fabsf(vp) > d.half_v) return false;
-    if (!(x >= 0.f && x <= d.xmax && y >= 0.f && y <= d.ymax)) return false;
-    float tt = X * v.s + Y * v.c;
-    float dd = fabsf(ts - v.tanb * tt) * v.rs;
-    if (ts < 0.f) dd = -dd;
-    float den = d.D - dd;
-    *w = (d.D * d.D) / (den * den);
+  const bool near = c.near || fabsf(fabsf(vp) - d.half_v) < 1e-4f * d.half_v ||
+                    fabsf(x - d.xmax) < 1e-3f || fabsf(x) < 1e-3f;
+  if (!near) {
+    if (c.out || fabsf(vp) > d.half_v || !(x >= 0.f && x <= d.xmax)) return false;
+    *w = c.w;
     *xi = (int)x;
-    *yi = (int)y;
+    *yi = c.yi;
     *fx = x - (float)*xi;
-    *fy = y - (float)*yi;
+    *fy = c.fy;
     return true;
   }
   double xd, yd, wd;
@@ -247,6 +267,15 @@ __device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const 
   *fx = (float)(xd - *xi);
   *fy = (float)(yd - *yi);
   return true;
+}
+
+// bp_column + bp_coef_z for one voxel.
+__device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const BpViewD& vd, int s,
+                                        int t, int z, float X, float Y, float Z, int* xi, int* yi,
+                                        float* fx, float* fy, float* w) {
+  BpColumn c;
+  bp_column(d, v, X, Y, &c);
+  return bp_coef_z(d, c, vd, s, t, z, Z, xi, yi, fx, fy, w);
 }
 
 // Bilinear read at integer corner (xi, yi) with fractions (fx, fy), with the

@@ -4,13 +4,16 @@
 //  * Forward projector = transpose of the voxel-driven backprojection
 //    (recon/bp3d20.cpp:81-166): G[k][row][col] = sum over voxels of
 //    w * factor * (bilinear weight of (row, col)) * R[z][t][s], with the
-//    coefficients of bp_coef, the function the plain backprojector uses.
-//    Ray-driven: a CTA owns one view and a block of detector columns; it
-//    enumerates the voxel columns in the wedge of source rays that project
-//    onto its detector columns (for each voxel row along the view's major
-//    axis, the range along the other axis follows from the perspective
-//    map), walks each candidate column along z, and accumulates into a
-//    shared-memory copy of its detector columns before one coalesced store.
+//    coefficients of bp_column + bp_coef_z, the operations the plain
+//    backprojector's bp_coef performs.  A CTA owns one view and a block of
+//    32 detector columns; it enumerates the voxel columns in the wedge of
+//    source rays that project onto them (for each voxel row along the
+//    view's major axis, the range along the other axis follows from the
+//    perspective map).  A warp takes one voxel column at a time with its
+//    lanes along z: the column's part of the coefficients is computed once,
+//    the lanes read 32 consecutive voxels of a z-major copy of the volume,
+//    and scatter into consecutive detector rows of a column-major shared
+//    accumulator (different banks), stored once, coalesced, at the end.
 //  * Adjoint of the weighting + ramp filter (recon/bp3d20.cpp:36-73): the
 //    Toeplitz matrix is symmetric, so the transpose filters along u again,
 //    reading [view][v][u] and writing [view][u][v], then applies the cosine
@@ -23,11 +26,13 @@ namespace {
 constexpr int FP_COLS = 32;    // detector columns per CTA
 constexpr int FP_THREADS = 256;
 
+// vol_z: the volume transposed to [s][t][z] (z contiguous).
 __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* __restrict__ views,
                                                         const BpViewD* __restrict__ viewsd,
                                                         const float* __restrict__ vol,
+                                                        const float* __restrict__ vol_z,
                                                         float* __restrict__ out) {
-  extern __shared__ float G[];  // [nv][FP_COLS]
+  extern __shared__ float G[];  // [FP_COLS][nv]: column-major
   const int k = blockIdx.y;
   const int c0 = blockIdx.x * FP_COLS;
   const int ncols = min(FP_COLS, d.nu - c0);
@@ -72,19 +77,18 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
       lo = max((int)floorf(fminf(sA, sB)) - 2, d.s_begin);
       hi = min((int)ceilf(fmaxf(sA, sB)) + 2, d.s_end - 1);
     }
-    for (int q = lo + lane; q <= hi; q += 32) {
+    for (int q = lo; q <= hi; q++) {  // warp-uniform: one voxel column at a time
       const int s = x_major ? d.s_begin + m : q;
       const int t = x_major ? q : m;
       const float X = fmaf((float)s, d.dvox, d.x0);
       const float Y = fmaf(-(float)t, d.dvox, d.y0);
-      // cheap column test: does this voxel column project near our columns?
-      {
-        float Vx, Vy;
-        bp_view_frame(d, v, X, Y, &Vx, &Vy);
-        float y = (d.half_u - Vy * (d.sdd / Vx)) * d.inv_du;
-        if (!(y >= (float)(c0 - 2) && y < (float)(c0 + ncols + 1))) continue;
-      }
-      for (int z = 0; z < d.nz; z++) {
+      // the column's part of the coefficients, once; does it project near
+      // our detector columns (margin 2)?
+      BpColumn col;
+      bp_column(d, v, X, Y, &col);
+      if (!(col.y >= (float)(c0 - 2) && col.y < (float)(c0 + ncols + 1))) continue;
+      const float* src = vol_z + ((size_t)s * d.ny + t) * d.nz;
+      for (int z = lane; z < d.nz; z += 32) {
         if (d.mask_r2 > 0) {
           int a = z - d.cz, b = t - d.ct, c = s - d.cs;
           if (a * a + b * b + c * c > d.mask_r2) continue;
@@ -92,21 +96,21 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
         const float Z = fmaf(-(float)z, d.dvox, d.z0);
         int xi, yi;
         float fx, fy, w;
-        if (!bp_coef(d, v, vd, s, t, z, X, Y, Z, &xi, &yi, &fx, &fy, &w)) continue;
-        const float r = __ldg(vol + ((size_t)z * d.ny + t) * d.nx + s);
+        if (!bp_coef_z(d, col, vd, s, t, z, Z, &xi, &yi, &fx, &fy, &w)) continue;
+        const float r = __ldg(src + z);
         if (r == 0.f) continue;
         const float c = w * r * v.factor;
 #pragma unroll
         for (int dy = 0; dy < 2; dy++) {
-          const int col = yi + dy - c0;
-          if (col < 0 || col >= ncols || yi + dy >= d.nu) continue;
+          const int cl = yi + dy - c0;
+          if (cl < 0 || cl >= ncols || yi + dy >= d.nu) continue;
           const float wy = dy ? fy : 1.f - fy;
 #pragma unroll
           for (int dx = 0; dx < 2; dx++) {
             const int row = xi + dx;
             if (row >= d.nv) continue;
             const float wx = dx ? fx : 1.f - fx;
-            atomicAdd(&G[row * FP_COLS + col], c * wx * wy);
+            atomicAdd(&G[cl * d.nv + row], c * wx * wy);
           }
         }
       }
@@ -115,8 +119,26 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
   __syncthreads();
   float* dst = out + (size_t)k * d.nu * d.nv;
   for (int i = threadIdx.x; i < d.nv * FP_COLS; i += FP_THREADS) {
-    int row = i / FP_COLS, col = i % FP_COLS;
-    if (col < ncols) dst[(size_t)row * d.nu + c0 + col] = G[i];
+    int row = i / FP_COLS, cl = i % FP_COLS;
+    if (cl < ncols) dst[(size_t)row * d.nu + c0 + cl] = G[cl * d.nv + row];
+  }
+}
+
+// out[s][t][z] = in[z][t][s]: per t, a 32 x 32 tile of the (z, s) plane
+// through shared memory, read along s and written along z
+__global__ void transpose_zs_kernel(int nx, int ny, int nz, const float* __restrict__ in,
+                                    float* __restrict__ out) {
+  __shared__ float tile[32][33];
+  const int t = blockIdx.z;
+  const int s0 = blockIdx.x * 32, z0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const int z = z0 + i, s = s0 + threadIdx.x;
+    if (z < nz && s < nx) tile[i][threadIdx.x] = in[((size_t)z * ny + t) * nx + s];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const int s = s0 + i, z = z0 + threadIdx.x;
+    if (z < nz && s < nx) out[((size_t)s * ny + t) * nz + z] = tile[threadIdx.x][i];
   }
 }
 
@@ -178,13 +200,18 @@ __global__ void __launch_bounds__(256) filter_adjoint_kernel(int nu, int nv,
 }  // namespace
 
 cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
-                                       const float* vol, float* out, cudaStream_t st) {
+                                       const float* vol, float* vol_z, float* out,
+                                       cudaStream_t st) {
+  if (!vol_z) return cudaErrorInvalidValue;
+  dim3 tg((d.nx + 31) / 32, (d.nz + 31) / 32, d.ny);
+  transpose_zs_kernel<<<tg, dim3(32, 8), 0, st>>>(d.nx, d.ny, d.nz, vol, vol_z);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
   size_t smem = (size_t)d.nv * FP_COLS * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(fp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  e = cudaFuncSetAttribute(fp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   dim3 grid((d.nu + FP_COLS - 1) / FP_COLS, d.n_views);
-  fp_kernel<<<grid, FP_THREADS, smem, st>>>(d, views, viewsd, vol, out);
+  fp_kernel<<<grid, FP_THREADS, smem, st>>>(d, views, viewsd, vol, vol_z, out);
   return cudaGetLastError();
 }
 

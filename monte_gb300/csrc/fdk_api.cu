@@ -460,8 +460,11 @@ int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const flo
     dv = (const float*)ctx->scratch[kScratchVolXY].ptr;
     dout = (float*)ctx->scratch[kScratchFiltered].ptr;
   }
+  // z-major copy of the volume: the projector reads a voxel column along z
+  MONTE_TRY(ensure_slot(ctx, kScratchVolZY, vb, "z-major volume copy"));
   cudaError_t e = launch_fdk_forward_project(d, (const BpView*)ctx->fdk_views.ptr,
-                                             (const BpViewD*)ctx->fdk_viewsd.ptr, dv, dout,
+                                             (const BpViewD*)ctx->fdk_viewsd.ptr, dv,
+                                             (float*)ctx->scratch[kScratchVolZY].ptr, dout,
                                              ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "forward projection launch");
   if (mem == MONTE_MEM_HOST) {
@@ -497,8 +500,10 @@ int monte_fdk_backward(monte_ctx* ctx, const monte_fdk_geom* g, const float* gra
     dv = (const float*)ctx->scratch[kScratchVolXY].ptr;
     dout = (float*)ctx->scratch[kScratchProj].ptr;
   }
+  MONTE_TRY(ensure_slot(ctx, kScratchVolZY, vb, "z-major volume copy"));
   cudaError_t e = launch_fdk_forward_project(d, (const BpView*)ctx->fdk_views.ptr,
-                                             (const BpViewD*)ctx->fdk_viewsd.ptr, dv, tmp,
+                                             (const BpViewD*)ctx->fdk_viewsd.ptr, dv,
+                                             (float*)ctx->scratch[kScratchVolZY].ptr, tmp,
                                              ctx->stream);
   if (e == cudaSuccess)
     e = launch_fdk_filter_adjoint(d, tmp, (const float*)ctx->fdk_weights.ptr,
