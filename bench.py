@@ -209,24 +209,47 @@ MC_WORKLOAD = ("mc: 325^3 labels @0.8mm (water / Ca-water bone 1.5-1.9 / air, 20
                "SDD 1000 mm, 509 histories per pixel per view (1.0e8 per view), 5 interactions")
 
 
-def mc_inputs(device):
-    import torch
+def mc_workload():
+    """Geometry, host labels and an inputs factory (labels -> abi.McInputs)
+    of the 325^3 Monte Carlo workload."""
     from monte_gb300 import abi, phantoms
     x = np.load(os.path.join(REPO, "tests", "golden", "xcom.npz"))
     lab, vox, org, dens, mats = phantoms.ellipsoid_labels()
     E = np.arange(20.0, 81.0)
-    inp = abi.McInputs(torch.from_numpy(lab).to(device), vox, org, mats, dens,
-                       [x["water"], x["ca"]], E, 80.0 - E)
+
+    def make(labels):
+        return abi.McInputs(labels, vox, org, mats, dens, [x["water"], x["ca"]], E, 80.0 - E)
+
     g = abi.mc_geom(360, 512, 384, 0.08, 50.0, 100.0, 14.0, flags=abi.MONTE_MC_STALE_SIN_PHI)
-    return g, inp
+    return g, lab, make
 
 
-def mc_bench(ctx, device, steps=3, per=509):
+def mc_cpu_baseline(g, inp, per=256):
+    """The CPU replay harness (oracle/mc_oracle.c: the reference kernel's
+    history loop restated, the same step functions and streams, all host
+    cores) on a bounded sample of the 325^3 workload: view 0, the central
+    64 x 64 pixels, `per` histories each (1.05e6 histories)."""
+    import oracle
+    from monte_gb300 import abi
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    u0, v0 = g.nu // 2 - 32, g.nv // 2 - 32
+    req = abi.mc_request(2024, per, (0, 1), (u0, u0 + 64), (v0, v0 + 64))
+    t0 = time.perf_counter()
+    _, _, st = oracle.mc_run(g, inp, req)
+    dt = time.perf_counter() - t0
+    return {"value": st["histories"] / dt, "unit": "histories/s", "cores": cores, "kind": "port",
+            "sample": "CPU replay of view 0, central 64x64 pixels, %d histories each "
+                      "(%d histories, %.1f s)" % (per, st["histories"], dt)}
+
+
+def mc_bench(ctx, device, steps=3, per=509, with_cpu=True):
     """Histories/s of the persistent and the plain Monte Carlo kernels on one
     view of the 325^3 workload (1.0e8 histories per step)."""
     import torch
     from monte_gb300 import abi
-    g, inp = mc_inputs(device)
+    g, lab, make = mc_workload()
+    inp = make(torch.from_numpy(lab).to(device))
     prim = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device=device)
     scat = torch.zeros_like(prim)
     out = {"metric": "MC histories/s", "unit": "histories/s", "workload": MC_WORKLOAD}
@@ -250,6 +273,8 @@ def mc_bench(ctx, device, steps=3, per=509):
                      "interactions_per_history": st["interactions"] / st["histories"]}
     out["value"] = out["persistent"]["value"]
     out["persistent_over_plain"] = out["persistent"]["value"] / out["plain"]["value"]
+    if with_cpu:
+        out["cpu_baseline"] = mc_cpu_baseline(g, make(lab))
     return out
 
 
@@ -393,11 +418,15 @@ def run_reference(args):
             vals.append(cb["value"])
     v = statistics.median(vals)
     cb["value"] = v
+    mg, mlab, mmake = mc_workload()
+    mc_cb = mc_cpu_baseline(mg, mmake(mlab))
     line = {"impl": "reference", "metric": "FDK GUPS (voxel-view updates/s)", "value": v,
             "unit": "GUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": WORKLOAD},
             "cpu_baseline": cb,
+            "mc": {"metric": "MC histories/s", "unit": "histories/s", "value": mc_cb["value"],
+                   "workload": MC_WORKLOAD, "cpu_baseline": mc_cb},
             "e2e": {"value": v, "unit": "GUPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -548,7 +577,7 @@ def run_ours(args):
                              "ms_per_step": t_plain * 1e3,
                              "tuned_over_plain": value / world / (updates / t_plain / 1e9)}
     if not args.no_mc:
-        line["mc"] = mc_bench(ctx, dev)
+        line["mc"] = mc_bench(ctx, dev, with_cpu=rank == 0 and not args.no_cpu_baseline)
         line["gpu_launches_mc"] = 2 * 4
     if not args.no_batch and not args.small:
         line["batch"] = batch_bench(ctx, dev, args.batch_scale)

@@ -111,11 +111,10 @@ __global__ void __launch_bounds__(128) mc_plain_kernel(McDev d) {
   warp_stats(d, st);
 }
 
-// 64 registers: four CTAs (32 warps) per SM; measured against 80 registers
-// (three CTAs) and a four-step flight with the label reads issued together,
-// this form has the highest throughput: the kernel is bound by issue, not by
-// the latency of the label gathers
-__global__ void __launch_bounds__(256, 4) mc_persistent_kernel(McDev d) {
+// Body of the persistent kernel: SR Woodcock steps per round at most,
+// collisions processed once CB lanes of the warp wait (or none flies).
+template <int SR, int CB>
+__device__ __forceinline__ void persistent_body(const McDev& d) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -162,7 +161,7 @@ __global__ void __launch_bounds__(256, 4) mc_persistent_kernel(McDev d) {
     if (__all_sync(FULL, retired)) break;
     // ---- a few Woodcock steps ------------------------------------------
 #pragma unroll 1
-    for (int i = 0; i < kStepsPerRound && p.state == MC_FLY; i++) {
+    for (int i = 0; i < SR && p.state == MC_FLY; i++) {
       mc_flight_step(&d.P, d.T, d.labels, &p);
       st[1]++;
       if (p.state == MC_DEAD) st[5]++;
@@ -188,12 +187,20 @@ __global__ void __launch_bounds__(256, 4) mc_persistent_kernel(McDev d) {
     // ---- real collisions, processed as a batch ---------------------------
     const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
     const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
-    if (coll && (__popc(coll) >= kCollideBatch || fly == 0)) {
+    if (coll && (__popc(coll) >= CB || fly == 0)) {
       if (p.state == MC_COLLIDED) p.state = mc_after_collision(&d.P, d.T, &p);
     }
   }
   st[2] += (unsigned long long)p.n_int;
   warp_stats(d, st);
+}
+
+// 64 registers: four CTAs (32 warps) per SM.  Measured against 80 registers
+// (three CTAs) and a four-step flight with the label reads issued together,
+// this form has the highest throughput: the kernel is bound by issue, not by
+// the latency of the label gathers.
+__global__ void __launch_bounds__(256, 4) mc_persistent_kernel(McDev d) {
+  persistent_body<kStepsPerRound, kCollideBatch>(d);
 }
 
 // The persistent kernel over the histories of many jobs (phantoms of their
