@@ -11,6 +11,7 @@ is GUPS: voxel-view updates (325^3 * 360) per second.
          stream (inputs 283 MB > L2, so no extra L2 flush)
   e2e    the same call through the C ABI with pinned host buffers: the
          projection upload and the volume download are inside each step
+         (monte_fdk overlaps them with the filter and the backprojection)
   --impl reference  the CPU oracle (a restatement of recon/bp3d20.cpp) on
          all host cores over a bounded sample, scaled to GUPS
 
@@ -511,6 +512,7 @@ def run_ours(args):
     t_e2e = time.perf_counter() - t0
     t_e2e = max_over_ranks(t_e2e, world, dev)
     e2e_val = world * updates * n_e2e / t_e2e / 1e9
+    e2e_ranges = ctx.last_host_ranges()
     del h_vol
 
     peaks = {}
@@ -553,7 +555,8 @@ def run_ours(args):
                          "frac": bp_bytes / t_bp / 1e9 / hbm_peak, "traffic": traffic},
         "e2e": {"value": e2e_val, "unit": "GUPS",
                 "h2d_bytes_per_step": int(g.n_views * g.nu * g.nv * 4),
-                "d2h_bytes_per_step": int(g.nx * g.ny * g.nz * 4)},
+                "d2h_bytes_per_step": int(g.nx * g.ny * g.nz * 4),
+                "pipeline_view_ranges": e2e_ranges},
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }

@@ -141,9 +141,18 @@ int monte_fdk_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
 int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* filtered,
                           float* vol_xy, float* vol_zy, int bp_mode, int mem);
 /* Full FDK: filter then backproject.  `filtered` may be NULL (device scratch
- * owned by the context is used instead).  recon/bp3d20.cpp:15-194. */
+ * owned by the context is used instead).  recon/bp3d20.cpp:15-194.
+ * With MONTE_MEM_HOST, MONTE_BP_TILED, a full-width volume (s_begin 0,
+ * s_end nx) and every host buffer pinned (cudaHostAlloc / cudaHostRegister),
+ * the call is pipelined: the views are uploaded in ranges on a copy stream,
+ * each range filtered as it lands and backprojected into running sums, and
+ * the last range writes the volume straight into the pinned buffers.  The
+ * results equal the unpipelined path's bit for bit. */
 int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
               float* vol_xy, float* vol_zy, int filter_mode, int bp_mode, int mem);
+/* View ranges of the last monte_fdk call of this context that used host
+ * memory: >= 1 when it ran pipelined, 0 when it ran unpipelined. */
+int monte_fdk_last_host_ranges(const monte_ctx* ctx);
 
 /* Exact adjoint of monte_fdk_backproject (MONTE_BP_PLAIN coefficients): the
  * ray-driven cone-beam forward projector, vol_xy[nz][ny][nx] ->

@@ -122,6 +122,8 @@ int monte_ctx_destroy(monte_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   if (ctx->stream && ctx->stream != ctx->own_stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in);
+  if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out);
   for (auto& b : ctx->scratch) monte::release(b);
   monte::release(ctx->fdk_views);
   monte::release(ctx->fdk_viewsd);
@@ -132,6 +134,10 @@ int monte_ctx_destroy(monte_ctx* ctx) {
   monte::release(ctx->mc_views);
   monte::release(ctx->mc_pixels);
   if (ctx->d_status) cudaFree(ctx->d_status);
+  for (cudaEvent_t ev : ctx->pipe_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
+  if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return MONTE_OK;

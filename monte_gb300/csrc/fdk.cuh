@@ -97,10 +97,21 @@ bool bf16x3_supported(const FdkDev& d);
 cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
                                 const float* filtered, float* vol_xy, float* vol_zy,
                                 cudaStream_t st);
-// status: device int set to 1 if a bounded wait gave up (MONTE_ETIMEOUT)
+// One part of a backprojection: views [k_begin, k_end) of the geometry,
+// the per-voxel sums starting from acc_in ([z][y][x], the sums over the
+// views before k_begin) or from zero when acc_in is null.  Every voxel
+// accumulates its views in index order whatever the split, so the parts
+// of a backprojection give bit for bit the values of a single launch.
+struct BpPart {
+  int k_begin, k_end;
+  const float* acc_in;
+};
+// status: device int set to 1 if a bounded wait gave up (MONTE_ETIMEOUT);
+// part: NULL for all views from zero
 cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
                                 const float* filtered, float* vol_xy, float* vol_zy,
-                                int variant, int* status, cudaStream_t st);
+                                int variant, int* status, cudaStream_t st,
+                                const BpPart* part = nullptr);
 // Adjoints (fdk_adjoint.cu): forward projector = transpose of the plain
 // backprojector, into filtered-space layout [view][v][u] (vol_z: scratch of
 // the volume's size for its z-major copy); adjoint of the weighting +

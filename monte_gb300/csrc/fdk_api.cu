@@ -6,6 +6,7 @@
 // weights, filters, backprojects and writes three raw files
 // (recon/bp3d20.cpp:15-194).  Here the same three stages run on the GPU
 // behind monte_fdk_filter / monte_fdk_backproject / monte_fdk.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -289,6 +290,152 @@ size_t vol_bytes(const monte_fdk_geom* g) {
   return (size_t)g->nx * g->ny * g->nz * sizeof(float);
 }
 
+// ---- FDK from and to host memory, pipelined -------------------------------
+//
+// The views are cut into ranges that grow eightfold, the first about 1/90
+// of the scan (360 views: 0-4, 4-36, 36-360).  Range i is uploaded on copy_in, filtered on the context's
+// stream as soon as it has landed, and backprojected into the running
+// per-voxel sums (BpPart; one view behind, as the flat-edge reads of a
+// view's last row reach into the next view); the upload of range i+1 runs under the
+// backprojection of range i, so of the upload only the first, small range
+// stays on the critical path.  The last range's backprojection stores its
+// sums straight into the caller's pinned volume, which spreads the download
+// over that launch instead of appending it.  Filtered projections, when
+// asked for, go back range by range on copy_out.  The values are those of
+// the unsplit path bit for bit: the filter is per view, and every voxel sums
+// its views in index order.
+constexpr int kPipeMaxRanges = 8;
+enum { kEvStart = 0, kEvIn = 1, kEvFilt = 1 + kPipeMaxRanges, kEvOut = 1 + 2 * kPipeMaxRanges };
+static_assert(kEvOut < 24, "pipeline events");
+
+// Device address of pinned (page-locked, mapped) host memory, else null.
+void* host_mapped(const void* h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+int pipe_init(monte_ctx* ctx) {
+  if (ctx->pipe_ready) return MONTE_OK;
+  if (!ctx->copy_in)
+    MONTE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+  if (!ctx->copy_out)
+    MONTE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+  for (cudaEvent_t& ev : ctx->pipe_ev)
+    if (!ev) MONTE_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  ctx->pipe_ready = true;
+  return MONTE_OK;
+}
+
+// View ranges [r[i], r[i+1]) of the pipeline; returns their number.
+int pipe_ranges(int n_views, int* r) {
+  int nr = 0, b = 0, len = std::max(1, (n_views + 89) / 90);
+  r[0] = 0;
+  while (b < n_views) {
+    int e = std::min(n_views, b + len);
+    if (nr == kPipeMaxRanges - 1 || n_views - e < len) e = n_views;  // fold a short tail in
+    r[++nr] = e;
+    b = e;
+    len *= 8;
+  }
+  return nr;
+}
+
+int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
+                            float* filtered, float* dvol_xy, float* dvol_zy, int filter_mode,
+                            int variant) {
+  const size_t view_elems = (size_t)g->nu * g->nv;
+  const size_t pb = proj_bytes(g), vb = vol_bytes(g);
+  int r[kPipeMaxRanges + 1];
+  const int nr = pipe_ranges(g->n_views, r);
+  MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
+  MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
+  if (nr > 1) MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "partial sums"));
+  float* dp = (float*)ctx->scratch[kScratchProj].ptr;
+  float* df = (float*)ctx->scratch[kScratchFiltered].ptr;
+  float* dsum = (float*)ctx->scratch[kScratchVolXY].ptr;
+  cudaEvent_t* ev = ctx->pipe_ev;
+  // the copies start after the work already queued on the stream (which
+  // may still read the staging buffers)
+  MONTE_CUDA(ctx, cudaEventRecord(ev[kEvStart], ctx->stream));
+  MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_in, ev[kEvStart], 0));
+  MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvStart], 0));
+  for (int i = 0; i < nr; i++) {
+    const size_t off = (size_t)r[i] * view_elems;
+    MONTE_CUDA(ctx, cudaMemcpyAsync(dp + off, proj + off,
+                                    (size_t)(r[i + 1] - r[i]) * view_elems * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx->copy_in));
+    MONTE_CUDA(ctx, cudaEventRecord(ev[kEvIn + i], ctx->copy_in));
+  }
+  const FdkDev d = make_fdk_dev(*g);
+  const BpView* views = (const BpView*)ctx->fdk_views.ptr;
+  const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
+  bool have_sum = false;  // dsum holds the sums of the views before this range
+  for (int i = 0; i < nr; i++) {
+    const size_t off = (size_t)r[i] * view_elems;
+    const size_t bytes = (size_t)(r[i + 1] - r[i]) * view_elems * sizeof(float);
+    MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvIn + i], 0));
+    monte_fdk_geom gr = *g;  // the range's views as a scan of their own
+    gr.n_views = r[i + 1] - r[i];
+    MONTE_TRY(run_filter(ctx, &gr, dp + off, df + off, filter_mode));
+    if (filtered) {
+      MONTE_CUDA(ctx, cudaEventRecord(ev[kEvFilt + i], ctx->stream));
+      MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvFilt + i], 0));
+      MONTE_CUDA(ctx, cudaMemcpyAsync(filtered + off, df + off, bytes, cudaMemcpyDeviceToHost,
+                                      ctx->copy_out));
+    }
+    // the backprojection ranges trail the filtered ones by a view: with
+    // the flat-edge reads (MONTE_FDK_FLAT_EDGE) view k's last row and
+    // column read on into view k + 1
+    const bool last = i == nr - 1;
+    const int kb = i == 0 ? 0 : r[i] - 1, ke = last ? g->n_views : r[i + 1] - 1;
+    if (ke == kb && !last) continue;
+    const BpPart part{kb, ke, have_sum ? dsum : nullptr};
+    cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, last ? dvol_xy : dsum,
+                                        last ? dvol_zy : nullptr, variant, ctx->d_status,
+                                        ctx->stream, &part);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "backprojection launch");
+    have_sum = true;
+  }
+  ctx->last_bp_variant = variant;
+  ctx->last_host_ranges = nr;
+  MONTE_CUDA(ctx, cudaEventRecord(ev[kEvOut], ctx->copy_out));
+  MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvOut], 0));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MONTE_OK;
+}
+
+// Runs the pipelined path and returns 1 when the call qualifies for it:
+// tiled backprojection of full-width volumes, all host buffers pinned.
+// Returns 0 (nothing done) otherwise.
+int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
+                       float* filtered, float* vol_xy, float* vol_zy, int filter_mode, int bp_mode,
+                       int* rc) {
+  if (bp_mode != MONTE_BP_TILED || g->s_begin != 0 || g->s_end != g->nx) return 0;
+  if (filter_mode != MONTE_FILTER_FP32 && filter_mode != MONTE_FILTER_BF16X3) return 0;
+  const FdkDev d = make_fdk_dev(*g);
+  int variant = ctx->bp_tune_choice;
+  if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
+  if (!fdk_bp_tiled_supported(d, variant)) return 0;
+  float* mxy = (float*)host_mapped(vol_xy);
+  float* mzy = vol_zy ? (float*)host_mapped(vol_zy) : nullptr;
+  if (!mxy || (vol_zy && !mzy) || !host_mapped(proj) || (filtered && !host_mapped(filtered)))
+    return 0;
+  *rc = pipe_init(ctx);
+  if (*rc == MONTE_OK)
+    *rc = fdk_host_pipelined_body(ctx, g, proj, filtered, mxy, mzy, filter_mode, variant);
+  if (*rc != MONTE_OK) {
+    // nothing may still read or write the caller's buffers after the return
+    cudaStreamSynchronize(ctx->copy_in);
+    cudaStreamSynchronize(ctx->copy_out);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  return 1;
+}
+
 }  // namespace
 }  // namespace monte
 
@@ -395,6 +542,12 @@ int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float*
     MONTE_TRY(run_filter(ctx, g, proj, df, filter_mode));
     return run_bp(ctx, g, df, vol_xy, vol_zy, bp_mode);
   }
+  int rc = MONTE_OK;
+  ctx->last_host_ranges = 0;
+  if (fdk_host_pipelined(ctx, g, proj, filtered, vol_xy, vol_zy, filter_mode, bp_mode, &rc))
+    return rc;
+  // pageable buffers, the plain backprojector or a column window: one
+  // upload, the two stages, one download
   MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
   MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
   MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "volume staging"));
@@ -435,6 +588,8 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
 }
 
 int monte_fdk_last_bp_variant(const monte_ctx* ctx) { return ctx ? ctx->last_bp_variant : -1; }
+
+int monte_fdk_last_host_ranges(const monte_ctx* ctx) { return ctx ? ctx->last_host_ranges : 0; }
 
 int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const float* vol_xy,
                               float* filtered_out, int mem) {

@@ -32,8 +32,8 @@ namespace monte {
 namespace {
 
 constexpr int kChunk = 64;          // histories claimed per warp atomic
-constexpr int kStepsPerRound = 4;   // Woodcock steps per flight per round
-constexpr int kCollideBatch = 12;   // interact once this many lanes wait
+constexpr int kStepsPerRound = 16;  // Woodcock steps per flight per round
+constexpr int kCollideBatch = 4;    // interact once this many lanes wait
 
 __device__ __forceinline__ void decompose(const McDev& d, unsigned long long h, int* view,
                                           int* iu, int* iv, unsigned long long* k) {

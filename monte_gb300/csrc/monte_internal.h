@@ -47,6 +47,12 @@ struct monte_ctx {
   std::vector<uint8_t> bp_tune_key;
   int bp_tune_choice = -1;
   int last_bp_variant = -1;  // tile variant of the last backprojection, -1: plain kernel
+  // host-memory FDK pipeline (created on first use): upload and download
+  // streams, and the events that order them against `stream`
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t pipe_ev[24] = {};
+  bool pipe_ready = false;
+  int last_host_ranges = 0;  // view ranges of the last pipelined monte_fdk, 0: unpipelined
 };
 
 namespace monte {

@@ -57,6 +57,7 @@ def load(build_if_missing=False):
     lib.monte_fdk_forward_project.argtypes = [P, G, P, P, C.c_int]
     lib.monte_fdk_backward.argtypes = [P, G, P, P, C.c_int]
     lib.monte_fdk_last_bp_variant.argtypes = [P]
+    lib.monte_fdk_last_host_ranges.argtypes = [P]
     lib.monte_fdk_set_bp_variant.argtypes = [P, C.c_int]
     lib.monte_ctx_check_status.argtypes = [P]
     MG = C.POINTER(abi.McGeom)
@@ -177,6 +178,10 @@ class Context:
 
     def last_bp_variant(self):
         return self.lib.monte_fdk_last_bp_variant(self.h)
+
+    def last_host_ranges(self):
+        """View ranges of the last host-memory fdk() (0: it ran unpipelined)."""
+        return self.lib.monte_fdk_last_host_ranges(self.h)
 
     def set_bp_variant(self, variant):
         self.check(self.lib.monte_fdk_set_bp_variant(self.h, variant))
