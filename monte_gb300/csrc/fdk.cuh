@@ -221,24 +221,37 @@ struct BpColumn {
   float w;         // D^2 / (D - d)^2
   float fy;        // column fraction
   int yi;          // column index
-  bool near;       // ts, u' or y near a discontinuity of the operator
+  bool near;       // u' or y near a discontinuity of the operator
   bool out;        // rejected whatever z (|u'| > half_u or y outside [0, ymax])
 };
 
-__device__ __forceinline__ void bp_column(const FdkDev& d, const BpView& v, float X, float Y,
-                                          BpColumn* c) {
+// Whether the reference's tmp_s (recon/bp3d20.cpp:134) is negative, with
+// its double arithmetic (the same operations as bp_ref_voxel).  The
+// distance weight changes sign with tmp_s, and that sign is the only
+// discontinuity of the weight; the float ts decides it when clear of 0,
+// this where it is not.  The value of the weight is continuous there, so
+// the float form stays exact enough: only the sign is taken from here.  A
+// column on the rotation axis (even grids) has ts ~ 0 in every view.
+__device__ __forceinline__ bool bp_ts_negative(const FdkDev& d, const BpViewD& v, int s, int t) {
+  const double X = __dadd_rn(d.x0d, __dmul_rn((double)s, d.dvoxd));
+  const double Y = __dsub_rn(d.y0d, __dmul_rn((double)t, d.dvoxd));
+  return __dsub_rn(__dmul_rn(X, v.c), __dmul_rn(Y, v.s)) < 0.0;
+}
+
+__device__ __forceinline__ void bp_column(const FdkDev& d, const BpView& v, const BpViewD& vd,
+                                          int s, int t, float X, float Y, BpColumn* c) {
   float Vx, Vy;
   bp_view_frame(d, v, X, Y, &Vx, &Vy);
   c->kk = d.sdd / Vx;
   c->up = Vy * c->kk;
   c->y = bp_scale(d.half_u - c->up, d.inv_du, d.inv_du_lo);
   c->ts = X * v.c - Y * v.s;
-  c->near = fabsf(c->ts) < 1e-4f || fabsf(fabsf(c->up) - d.half_u) < 1e-4f * d.half_u ||
+  c->near = fabsf(fabsf(c->up) - d.half_u) < 1e-4f * d.half_u ||
             fabsf(c->y - d.ymax) < 1e-3f || fabsf(c->y) < 1e-3f;
   c->out = fabsf(c->up) > d.half_u || !(c->y >= 0.f && c->y <= d.ymax);
   float tt = X * v.s + Y * v.c;
   float dd = fabsf(c->ts - v.tanb * tt) * v.rs;
-  if (c->ts < 0.f) dd = -dd;
+  if (fabsf(c->ts) < 1e-4f ? bp_ts_negative(d, vd, s, t) : c->ts < 0.f) dd = -dd;
   float den = d.D - dd;
   c->w = (d.D * d.D) / (den * den);
   c->yi = (int)c->y;
@@ -285,7 +298,7 @@ __device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const 
                                         int t, int z, float X, float Y, float Z, int* xi, int* yi,
                                         float* fx, float* fy, float* w) {
   BpColumn c;
-  bp_column(d, v, X, Y, &c);
+  bp_column(d, v, vd, s, t, X, Y, &c);
   return bp_coef_z(d, c, vd, s, t, z, Z, xi, yi, fx, fy, w);
 }
 

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
       // the column's part of the coefficients, once; does it project near
       // our detector columns (margin 2)?
       BpColumn col;
-      bp_column(d, v, X, Y, &col);
+      bp_column(d, v, vd, s, t, X, Y, &col);
       if (!(col.y >= (float)(c0 - 2) && col.y < (float)(c0 + ncols + 1))) continue;
       const float* src = vol_z + ((size_t)s * d.ny + t) * d.nz;
       for (int z = lane; z < d.nz; z += 32) {

@@ -173,3 +173,42 @@ def test_autotune_picks_a_tile_and_all_tiles_agree(ctx):
         v += 1
     assert v >= 12
     ctx.set_bp_variant(best)
+
+
+@pytest.mark.parametrize("bp_mode", BPS)
+def test_even_grid_axis_column_against_fp64_oracle(ctx, bp_mode):
+    """n even: voxel column n/2 lies on the rotation axis, where the
+    distance weight's sign term ts is ~0 in every view (decided in double,
+    as the reference computes it)."""
+    g = abi.fdk_geom_recon325(n_views=360, nu=128, nv=96, pitch_mm=3.2, n=80, voxel_mm=1.6)
+    proj = fdk_projections(g.n_views, g.nu, g.nv, 80)
+    _, xy = _run(ctx, g, proj, bp_mode=bp_mode)
+    v64 = oracle.fdk_backproject(g, oracle.fdk_filter(g, proj, precise=True))
+    assert rel_rms(xy, v64) < 1e-5
+    c = g.nx // 2
+    assert rel_rms(xy[:, c, c], v64[:, c, c]) < 1e-5
+
+
+def test_even_grid_backprojects_as_fast_as_odd(ctx):
+    """The axis column of an even grid once took the per-voxel double path
+    in every view; its warp then held the kernel for ~45 ms whatever the
+    volume size.  Even and odd grids of equal size must now take equal time."""
+    ms = {}
+    for n in (96, 97):
+        g = abi.fdk_geom_recon325(n_views=360, nu=128, nv=96, pitch_mm=3.2, n=n,
+                                  voxel_mm=1.6 * 80 / n)
+        filt = torch.rand((g.n_views, g.nv, g.nu), device="cuda") - 0.5
+        vol = torch.empty((g.nz, g.ny, g.nx), device="cuda")
+        ctx.fdk_backproject(g, filt, vol, mode=abi.MONTE_BP_TILED)
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            ctx.fdk_backproject(g, filt, vol, mode=abi.MONTE_BP_TILED)
+            e1.record()
+            torch.cuda.synchronize()
+            t.append(e0.elapsed_time(e1))
+        ctx.check_status()
+        ms[n] = sorted(t)[1]
+    assert ms[96] < 2.0 * ms[97], ms
