@@ -232,10 +232,15 @@ struct BpColumn {
 // this where it is not.  The value of the weight is continuous there, so
 // the float form stays exact enough: only the sign is taken from here.  A
 // column on the rotation axis (even grids) has ts ~ 0 in every view.
-__device__ __forceinline__ bool bp_ts_negative(const FdkDev& d, const BpViewD& v, int s, int t) {
-  const double X = __dadd_rn(d.x0d, __dmul_rn((double)s, d.dvoxd));
-  const double Y = __dsub_rn(d.y0d, __dmul_rn((double)t, d.dvoxd));
-  return __dsub_rn(__dmul_rn(X, v.c), __dmul_rn(Y, v.s)) < 0.0;
+// Out of line, with scalar arguments: inlined, the compiler evaluates the
+// double operations speculatively for every voxel-view (FP64 is slow on
+// this GPU), and a reference to the geometry would copy a by-value kernel
+// parameter to local memory.
+static __device__ __noinline__ bool bp_ts_negative(double x0d, double y0d, double dvoxd,
+                                                   const BpViewD* v, int s, int t) {
+  const double X = __dadd_rn(x0d, __dmul_rn((double)s, dvoxd));
+  const double Y = __dsub_rn(y0d, __dmul_rn((double)t, dvoxd));
+  return __dsub_rn(__dmul_rn(X, v->c), __dmul_rn(Y, v->s)) < 0.0;
 }
 
 __device__ __forceinline__ void bp_column(const FdkDev& d, const BpView& v, const BpViewD& vd,
@@ -251,7 +256,8 @@ __device__ __forceinline__ void bp_column(const FdkDev& d, const BpView& v, cons
   c->out = fabsf(c->up) > d.half_u || !(c->y >= 0.f && c->y <= d.ymax);
   float tt = X * v.s + Y * v.c;
   float dd = fabsf(c->ts - v.tanb * tt) * v.rs;
-  if (fabsf(c->ts) < 1e-4f ? bp_ts_negative(d, vd, s, t) : c->ts < 0.f) dd = -dd;
+  if (fabsf(c->ts) < 1e-4f ? bp_ts_negative(d.x0d, d.y0d, d.dvoxd, &vd, s, t) : c->ts < 0.f)
+    dd = -dd;
   float den = d.D - dd;
   c->w = (d.D * d.D) / (den * den);
   c->yi = (int)c->y;

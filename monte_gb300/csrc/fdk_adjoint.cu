@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
   for (int i = threadIdx.x; i < d.nv * FP_COLS; i += FP_THREADS) G[i] = 0.f;
   __syncthreads();
   const BpView v = views[k];
-  const BpViewD vd = viewsd[k];
+  const BpViewD& vd = viewsd[k];
   // u' range of the detector columns [c0 - 1, c0 + ncols] (one column of
   // margin either side), as y = (half_u - u') / du
   const float ua = d.half_u - (float)(c0 + ncols + 1) * (1.0f / d.inv_du);

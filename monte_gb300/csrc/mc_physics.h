@@ -63,6 +63,7 @@ typedef struct {
   float inv_dx, inv_dy, inv_dz;
   float clip_r2, clip_hz;    /* clip_r2 <= 0: no clip cylinder */
   uint64_t seed;
+  monte_philox_keys keys;    /* round keys of seed (monte_philox_schedule) */
   uint32_t job;
   uint64_t per;              /* histories per pixel per view */
   int view_begin, view_end, u_begin, u_end, v_begin, v_end;
@@ -164,7 +165,7 @@ MONTE_HD void mc_start(const mc_params* P, const mc_tables* T, const mc_view* V,
   /* spectrum (CBCT_real325im.cu:491-498): inverse CDF */
   float E = T->energy[0];
   if (T->n_lines > 1) {
-    float u = monte_uniform(&p->rng);
+    float u = monte_uniform_keys(&p->rng, &P->keys);
     int lo = 0, hi = T->n_lines - 1;
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
@@ -228,14 +229,14 @@ MONTE_HD int mc_label_at(const mc_params* P, const uint8_t* labels, float x, flo
  * probability mu(label)/mu_max.  Updates p->state. */
 MONTE_HD void mc_flight_step(const mc_params* P, const mc_tables* T, const uint8_t* labels,
                              mc_photon* p) {
-  float beta = monte_uniform(&p->rng);
+  float beta = monte_uniform_keys(&p->rng, &P->keys);
   float r = -monte_logf(beta) * T->inv_mu_max[p->kb];
   float dx, dy, dz;
   mc_dir(p, &dx, &dy, &dz);
   p->x = fmaf(r, dx, p->x);
   p->y = fmaf(r, dy, p->y);
   p->z = fmaf(r, dz, p->z);
-  float nu = monte_uniform(&p->rng);
+  float nu = monte_uniform_keys(&p->rng, &P->keys);
   int lab = mc_label_at(P, labels, p->x, p->y, p->z);
   p->steps++;
   if (lab < 0) {
@@ -281,7 +282,7 @@ MONTE_HD long long mc_detector_index(const mc_params* P, const mc_view* V, const
 MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
   int mat = T->label_material[p->label];
   if (mat < 0) return MC_DEAD;
-  float sc = monte_uniform(&p->rng);
+  float sc = monte_uniform_keys(&p->rng, &P->keys);
   p->n_int++;
   if (sc <= T->p_photo[mat][p->kb]) return MC_DEAD;
   if (sc <= T->p_photo_coh[mat][p->kb]) {
@@ -296,20 +297,20 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
   float ro = 1.0f;
   int ok = 0;
   for (int tries = 0; tries < MC_MAX_KN_TRIES; tries++) {
-    float r1 = monte_uniform(&p->rng);
+    float r1 = monte_uniform_keys(&p->rng, &P->keys);
     if (r1 < thr) {
-      float r2 = monte_uniform(&p->rng);
+      float r2 = monte_uniform_keys(&p->rng, &P->keys);
       ro = fmaf(2.0f / lambda, r2, 1.0f);
-      float r3 = monte_uniform(&p->rng);
+      float r3 = monte_uniform_keys(&p->rng, &P->keys);
       float inv = 1.0f / ro;
       if (r3 <= 4.0f * (inv - inv * inv)) {
         ok = 1;
         break;
       }
     } else {
-      float r2 = monte_uniform(&p->rng);
+      float r2 = monte_uniform_keys(&p->rng, &P->keys);
       ro = lam2 / fmaf(2.0f, 1.0f - r2, lambda);
-      float r3 = monte_uniform(&p->rng);
+      float r3 = monte_uniform_keys(&p->rng, &P->keys);
       float q = lambda - ro * lambda + 1.0f;
       if (r3 <= 0.5f * fmaf(q, q, 1.0f / ro)) {
         ok = 1;
@@ -325,7 +326,7 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
   p->E = 511.0f / lam_d;
   p->kb = mc_bin(p->E);
   float sphi, cphi;
-  monte_sincos_2pi(monte_uniform(&p->rng), &sphi, &cphi);
+  monte_sincos_2pi(monte_uniform_keys(&p->rng, &P->keys), &sphi, &cphi);
   /* incoming direction (:768-773; CBCT_real2.cpp:460-463) */
   float st = p->st, ct = p->ct, sp = p->sp, cp = p->cp;
   if ((P->flags & MC_F_FIRST_COMPTON_Z) && p->n_compton == 0) {

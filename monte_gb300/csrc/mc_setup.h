@@ -73,6 +73,7 @@ static inline int mc_setup_params(const monte_mc_geom* g, const monte_mc_phantom
   P->clip_r2 = ph->clip_radius > 0 ? (float)(ph->clip_radius * ph->clip_radius) : 0.0f;
   P->clip_hz = (float)ph->clip_half_z;
   P->seed = run->seed;
+  monte_philox_schedule(run->seed, &P->keys);
   P->job = run->job;
   P->per = run->histories_per_pixel;
   P->view_begin = run->view_begin;

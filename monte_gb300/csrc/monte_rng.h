@@ -60,6 +60,40 @@ MONTE_HD monte_u32x4 monte_philox4x32_10(monte_u32x4 c, uint32_t k0, uint32_t k1
   return c;
 }
 
+/* The round keys of key (k0, k1): round r uses (k0 + r W0, k1 + r W1).
+ * A kernel that runs one key reads them as constants instead of stepping
+ * the key in every round of every block; the outputs are the same. */
+typedef struct {
+  uint32_t k0[10], k1[10];
+} monte_philox_keys;
+
+MONTE_HD void monte_philox_schedule(uint64_t seed, monte_philox_keys* K) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; r++) {
+    K->k0[r] = k0;
+    K->k1[r] = k1;
+    k0 += MONTE_PHILOX_W0;
+    k1 += MONTE_PHILOX_W1;
+  }
+}
+
+MONTE_HD monte_u32x4 monte_philox4x32_10_keys(monte_u32x4 c, const monte_philox_keys* K) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; r++) {
+    uint64_t p0 = (uint64_t)MONTE_PHILOX_M0 * c.v[0];
+    uint64_t p1 = (uint64_t)MONTE_PHILOX_M1 * c.v[2];
+    monte_u32x4 n;
+    n.v[0] = (uint32_t)(p1 >> 32) ^ c.v[1] ^ K->k0[r];
+    n.v[1] = (uint32_t)p1;
+    n.v[2] = (uint32_t)(p0 >> 32) ^ c.v[3] ^ K->k1[r];
+    n.v[3] = (uint32_t)p0;
+    c = n;
+  }
+  return c;
+}
+
 /* One history's stream: block b of history h is
  * philox(counter = (b, h_lo, h_hi, job), key = (seed_lo, seed_hi)). */
 typedef struct {
@@ -100,11 +134,35 @@ MONTE_HD uint32_t monte_stream_u32(monte_stream* s) {
   return w == 0 ? s->buf[0] : w == 1 ? s->buf[1] : w == 2 ? s->buf[2] : s->buf[3];
 }
 
+/* monte_stream_u32 with the key's round keys precomputed (K must be the
+ * schedule of the stream's key). */
+MONTE_HD uint32_t monte_stream_u32_keys(monte_stream* s, const monte_philox_keys* K) {
+  uint32_t w = s->next & 3u;
+  if (w == 0) {
+    monte_u32x4 c;
+    c.v[0] = s->next >> 2;
+    c.v[1] = s->h_lo;
+    c.v[2] = s->h_hi;
+    c.v[3] = s->job;
+    monte_u32x4 r = monte_philox4x32_10_keys(c, K);
+    s->buf[0] = r.v[0];
+    s->buf[1] = r.v[1];
+    s->buf[2] = r.v[2];
+    s->buf[3] = r.v[3];
+  }
+  s->next++;
+  return w == 0 ? s->buf[0] : w == 1 ? s->buf[1] : w == 2 ? s->buf[2] : s->buf[3];
+}
+
 /* Uniform on (0, 1] with 24-bit resolution, like curand_uniform's range
  * (the reference's -log(beta) needs beta > 0, CBCT_real325im.cu:888-889). */
 MONTE_HD float monte_u01(uint32_t x) { return (float)((x >> 8) + 1u) * 5.9604644775390625e-8f; }
 
 MONTE_HD float monte_uniform(monte_stream* s) { return monte_u01(monte_stream_u32(s)); }
+
+MONTE_HD float monte_uniform_keys(monte_stream* s, const monte_philox_keys* K) {
+  return monte_u01(monte_stream_u32_keys(s, K));
+}
 
 /* ---- elementary functions ------------------------------------------ */
 

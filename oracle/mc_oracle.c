@@ -172,6 +172,8 @@ void oracle_compton(float E, uint64_t seed, int n, float* cos_theta, float* e_ou
     T->p_photo_coh[0][k] = 0.0f; /* always Compton */
   }
   P.max_int = 1000;
+  P.seed = seed;
+  monte_philox_schedule(seed, &P.keys);
   for (int i = 0; i < n; i++) {
     mc_photon p;
     memset(&p, 0, sizeof(p));
