@@ -177,11 +177,91 @@ MONTE_HD float monte_u2f(uint32_t u) {
   return f;
 }
 
-/* Natural log of a positive normal float.  x = 2^e * m, m in
- * [sqrt(1/2), sqrt(2)); log m = 2 atanh(s) with s = (m-1)/(m+1), summed as
- * the atanh Taylor series 2(s + s^3/3 + ... + s^11/11) (|s| <= 0.1716, the
- * truncation error is below 2e-11); e*ln2 is added in two parts (a
- * high part exact for |e| < 2^8 and the remainder).  Error about 1 ulp. */
+/* Natural log of a positive normal float, table-driven (the method of
+ * P. T. P. Tang, "Table-driven implementation of the logarithm function in
+ * IEEE floating-point arithmetic", ACM TOMS 16(4), 1990), with no division.
+ * x = 2^e m, m in [sqrt(1/2), sqrt(2)); the exponent and top mantissa bits
+ * of m pick one of 65 intervals, each with a float g close to 1/m (g = 1
+ * exactly for the two intervals next to 1, so log x keeps its relative
+ * accuracy as x -> 1).  Then r = m g - 1 (one fused rounding; |r| < 1/64)
+ * and log m = log1p(r) - log(g), log1p by its Taylor series to r^5
+ * (truncation below 3e-12 relative), -log(g) from the table as hi + lo
+ * floats; e ln2 is added in two parts (a high part exact for |e| < 2^8).
+ * Error below 2 ulp.  Row k of MONTE_LOG_TABLE: {g, -log(g) hi, lo, 0} for
+ * the m whose float bits b satisfy (b >> 17) == 0x1f9a + k; g = 2 / (m0 + m1)
+ * rounded to float over the interval [m0, m1], -log(g) from double. */
+#define MONTE_LOG_TABLE \
+  {0x1.690f88p+0f, -0x1.601f14p-2f, -0x1.1ac6f4p-28f, 0.0f}, \
+  {0x1.661ec8p+0f, -0x1.57bf7ap-2f, 0x1.c6e5c4p-27f, 0.0f}, \
+  {0x1.623fa8p+0f, -0x1.4c9e0cp-2f, 0x1.fa34f2p-28f, 0.0f}, \
+  {0x1.5e75bcp+0f, -0x1.419b44p-2f, 0x1.ca85dp-28f, 0.0f}, \
+  {0x1.5ac058p+0f, -0x1.36b67cp-2f, 0x1.683dep-27f, 0.0f}, \
+  {0x1.571ed4p+0f, -0x1.2bef08p-2f, -0x1.f724d4p-28f, 0.0f}, \
+  {0x1.539096p+0f, -0x1.21445cp-2f, 0x1.ae28eap-27f, 0.0f}, \
+  {0x1.501502p+0f, -0x1.16b5cep-2f, -0x1.a59f6ep-27f, 0.0f}, \
+  {0x1.4cab8ap+0f, -0x1.0c42dcp-2f, 0x1.83d3aap-27f, 0.0f}, \
+  {0x1.4953ap+0f, -0x1.01eaeap-2f, -0x1.c4d8cap-27f, 0.0f}, \
+  {0x1.460cbep+0f, -0x1.ef5ae8p-3f, 0x1.08c01cp-29f, 0.0f}, \
+  {0x1.42d664p+0f, -0x1.db13e6p-3f, 0x1.256ee6p-28f, 0.0f}, \
+  {0x1.3fb014p+0f, -0x1.c6ffbcp-3f, -0x1.1e01eep-28f, 0.0f}, \
+  {0x1.3c995cp+0f, -0x1.b31d9p-3f, -0x1.2b79b8p-28f, 0.0f}, \
+  {0x1.3991c4p+0f, -0x1.9f6c48p-3f, -0x1.2112c4p-28f, 0.0f}, \
+  {0x1.3698ep+0f, -0x1.8beb04p-3f, 0x1.31c064p-29f, 0.0f}, \
+  {0x1.33ae46p+0f, -0x1.7898dap-3f, -0x1.11131cp-29f, 0.0f}, \
+  {0x1.30d19p+0f, -0x1.6574ecp-3f, 0x1.2e7d98p-28f, 0.0f}, \
+  {0x1.2e025cp+0f, -0x1.527e5ep-3f, -0x1.50dac6p-30f, 0.0f}, \
+  {0x1.2b404cp+0f, -0x1.3fb462p-3f, -0x1.e64a22p-29f, 0.0f}, \
+  {0x1.288b02p+0f, -0x1.2d1616p-3f, -0x1.30d024p-28f, 0.0f}, \
+  {0x1.25e228p+0f, -0x1.1aa2bep-3f, -0x1.447eep-28f, 0.0f}, \
+  {0x1.234568p+0f, -0x1.08598ep-3f, -0x1.33c74p-28f, 0.0f}, \
+  {0x1.20b472p+0f, -0x1.ec73aap-4f, 0x1.bd7bdep-30f, 0.0f}, \
+  {0x1.1e2ef4p+0f, -0x1.c88584p-4f, -0x1.6f12c6p-30f, 0.0f}, \
+  {0x1.1bb4a4p+0f, -0x1.a4e764p-4f, 0x1.a721e4p-31f, 0.0f}, \
+  {0x1.194538p+0f, -0x1.8197e2p-4f, -0x1.d038fcp-30f, 0.0f}, \
+  {0x1.16e06ap+0f, -0x1.5e95bap-4f, 0x1.1a1bc4p-30f, 0.0f}, \
+  {0x1.1485f2p+0f, -0x1.3bdf6cp-4f, 0x1.c5c244p-29f, 0.0f}, \
+  {0x1.12359p+0f, -0x1.1973d4p-4f, -0x1.46545ep-32f, 0.0f}, \
+  {0x1.0fef02p+0f, -0x1.eea338p-5f, -0x1.01adecp-31f, 0.0f}, \
+  {0x1.0db20cp+0f, -0x1.aaef5ap-5f, 0x1.c13c3cp-31f, 0.0f}, \
+  {0x1.0b7e7p+0f, -0x1.67c976p-5f, 0x1.a568c2p-30f, 0.0f}, \
+  {0x1.0953f4p+0f, -0x1.252f4p-5f, -0x1.e34604p-31f, 0.0f}, \
+  {0x1.073262p+0f, -0x1.c63d84p-6f, 0x1.7d6b12p-31f, 0.0f}, \
+  {0x1.05198p+0f, -0x1.432ab2p-6f, -0x1.66031p-32f, 0.0f}, \
+  {0x1.03091cp+0f, -0x1.8244ep-7f, -0x1.c4506ep-34f, 0.0f}, \
+  {0x1.0p+0f, 0.0f, 0.0f, 0.0f}, \
+  {0x1.0p+0f, 0.0f, 0.0f, 0.0f}, \
+  {0x1.f4465cp-1f, 0x1.7b916cp-6f, -0x1.054992p-31f, 0.0f}, \
+  {0x1.ecc07ep-1f, 0x1.39e84cp-5f, 0x1.bfd7fp-30f, 0.0f}, \
+  {0x1.e573aep-1f, 0x1.b42dbep-5f, 0x1.a32e4ap-30f, 0.0f}, \
+  {0x1.de5d7p-1f, 0x1.16536p-4f, -0x1.5c84bp-32f, 0.0f}, \
+  {0x1.d77b66p-1f, 0x1.51b06ep-4f, -0x1.7cf3d8p-31f, 0.0f}, \
+  {0x1.d0cb5ap-1f, 0x1.8c3454p-4f, 0x1.0c66d2p-30f, 0.0f}, \
+  {0x1.ca4b32p-1f, 0x1.c5e53ap-4f, 0x1.5bc7b2p-32f, 0.0f}, \
+  {0x1.c3f8f2p-1f, 0x1.fec902p-4f, -0x1.20a598p-35f, 0.0f}, \
+  {0x1.bdd2bap-1f, 0x1.1b72a6p-3f, 0x1.c5ecfap-28f, 0.0f}, \
+  {0x1.b7d6c6p-1f, 0x1.371fb8p-3f, 0x1.1e8fd8p-31f, 0.0f}, \
+  {0x1.b20366p-1f, 0x1.526e54p-3f, 0x1.d43692p-28f, 0.0f}, \
+  {0x1.ac5704p-1f, 0x1.6d60f4p-3f, -0x1.5cc5acp-28f, 0.0f}, \
+  {0x1.a6d01cp-1f, 0x1.87f9fep-3f, 0x1.64192ap-28f, 0.0f}, \
+  {0x1.a16d4p-1f, 0x1.a23bcp-3f, -0x1.d4a99p-35f, 0.0f}, \
+  {0x1.9c2d16p-1f, 0x1.bc2862p-3f, -0x1.a4e61cp-32f, 0.0f}, \
+  {0x1.970e5p-1f, 0x1.d5c214p-3f, 0x1.a7ddccp-30f, 0.0f}, \
+  {0x1.920fb6p-1f, 0x1.ef0ad6p-3f, -0x1.48e9a6p-29f, 0.0f}, \
+  {0x1.8d301ap-1f, 0x1.040256p-2f, 0x1.0d3414p-28f, 0.0f}, \
+  {0x1.886e6p-1f, 0x1.1058bep-2f, -0x1.ca36a4p-27f, 0.0f}, \
+  {0x1.83c978p-1f, 0x1.1c898cp-2f, -0x1.92cccp-27f, 0.0f}, \
+  {0x1.7f406p-1f, 0x1.2895ap-2f, 0x1.7bd0d4p-27f, 0.0f}, \
+  {0x1.7ad222p-1f, 0x1.347dd6p-2f, -0x1.f3c146p-29f, 0.0f}, \
+  {0x1.767ddp-1f, 0x1.404304p-2f, -0x1.5e55fcp-28f, 0.0f}, \
+  {0x1.72428ap-1f, 0x1.4be5f4p-2f, -0x1.4221c8p-28f, 0.0f}, \
+  {0x1.6e1f78p-1f, 0x1.57676ep-2f, -0x1.5d52bcp-29f, 0.0f}, \
+  {0x1.6b0f96p-1f, 0x1.600112p-2f, 0x1.71fdcp-30f, 0.0f}
+
+#if defined(__CUDACC__)
+static __device__ const float4 monte_log_tbl_d[65] = {MONTE_LOG_TABLE};
+#endif
+static const float monte_log_tbl_h[65][4] = {MONTE_LOG_TABLE};
+
 MONTE_HD float monte_logf(float x) {
   uint32_t b = monte_f2u(x);
   int e = (int)((b >> 23) & 0xffu) - 127;
@@ -190,17 +270,19 @@ MONTE_HD float monte_logf(float x) {
     mb -= 0x00800000u;
     e += 1;
   }
+  const uint32_t k = (mb >> 17) - 0x1f9au;
+#if defined(__CUDA_ARCH__)
+  const float4 t = monte_log_tbl_d[k];
+  const float g = t.x, thi = t.y, tlo = t.z;
+#else
+  const float g = monte_log_tbl_h[k][0], thi = monte_log_tbl_h[k][1], tlo = monte_log_tbl_h[k][2];
+#endif
   float m = monte_u2f(mb);
-  float f = m - 1.0f;
-  float s = f / (m + 1.0f);
-  float z = s * s;
-  float p = 0.18181818181818182f;          /* 2/11 */
-  p = fmaf(p, z, 0.22222222222222222f);    /* 2/9 */
-  p = fmaf(p, z, 0.28571428571428571f);    /* 2/7 */
-  p = fmaf(p, z, 0.4f);                    /* 2/5 */
-  p = fmaf(p, z, 0.66666666666666667f);    /* 2/3 */
-  float t = s * z;
-  float lm = fmaf(t, p, 2.0f * s);
+  float r = fmaf(m, g, -1.0f);
+  float q = fmaf(r, 0.2f, -0.25f);
+  q = fmaf(q, r, 0.33333333333333333f);
+  q = fmaf(q, r, -0.5f);
+  float lm = thi + (tlo + fmaf(r * r, q, r));
   float fe = (float)e;
   /* ln2 = 0.693145751953125 (exact, 16 significant bits) + 1.428606820e-6 */
   return fmaf(fe, 0.693145751953125f, fmaf(fe, 1.42860682030941723212e-6f, lm));
