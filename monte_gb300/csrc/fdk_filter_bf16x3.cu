@@ -18,18 +18,21 @@
 // relative RMS of the FP64 oracle).
 //
 // Kernel shape.  One CTA computes a 128 x BN output tile (128 detector rows
-// of one view, BN columns) over K = nu in chunks of 64:
+// of one view, BN columns) over K = nu in chunks of 32, in 96 KB of shared
+// memory and BN TMEM columns, so that two CTAs share an SM (one converts
+// while the other's MMAs or epilogue run):
 //  * all 8 warps load the A chunk (fp32, coalesced along v), weight it,
 //    split it and store hi/lo into shared memory in the canonical K-major
 //    core-matrix layout (8 rows x 16 bytes per core matrix);
 //  * thread 0 brings the pre-split, pre-tiled B chunk (host-built, band
 //    removed) with two cp.async.bulk copies on an mbarrier, then issues the
-//    12 tcgen05.mma of the chunk and commits them to a second mbarrier;
+//    6 tcgen05.mma of the chunk (3 per 16-wide K step) and commits them to a second mbarrier;
 //  * two stages alternate, so the conversion of chunk k+1 overlaps the MMAs
 //    of chunk k;
-//  * epilogue: tcgen05.ld of the accumulator rows, plus the FP32 band from
-//    an fp32 copy of the A rows staged in the (now idle) shared memory, then
-//    float4 stores of the transposed output filtered[view][v][u].
+//  * epilogue, per window of 64 output columns: tcgen05.ld of the
+//    accumulator rows, plus the FP32 band from an fp32 copy of the window's
+//    A columns (and 16 either side) staged in the (now idle) shared memory,
+//    then float4 stores of the transposed output filtered[view][v][u].
 // Every wait is bounded; on timeout the CTA sets *status, drains and frees
 // its TMEM.
 #include <cuda_bf16.h>
@@ -44,7 +47,7 @@ namespace monte {
 
 namespace {
 
-constexpr int KC = 64;        // K per chunk
+constexpr int KC = 32;        // K per chunk
 constexpr int KBAND = 16;     // near field |c - b| <= KBAND handled in FP32
 constexpr int NTHREADS = 256;
 
@@ -62,7 +65,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 }
 
 template <int BN>
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(NTHREADS, 2)
     filter_bf16x3_kernel(int nu, int nv, const float* __restrict__ proj,
                          const float* __restrict__ weights, const uint16_t* __restrict__ bsplit,
                          const BandTaps band, float* __restrict__ out, int* status) {
@@ -70,7 +73,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr int B_BYTES = BN * KC * 2;         // one of hi / lo
   constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
   constexpr uint32_t IDESC = ptx::idesc_bf16_f32(128, BN);
-  constexpr int EPI = (BN + 2 * KBAND) * 128 * 4;  // fp32 A rows for the band
+  constexpr int WC = 64;                           // output columns per epilogue window
+  constexpr int KW = WC + 2 * KBAND;               // A columns staged per window
+  constexpr int EPI = KW * 128 * 4;                // fp32 A rows for the band
   constexpr int BAR_OFF = 2 * STAGE > EPI ? 2 * STAGE : EPI;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + BAR_OFF);  // b_full[2], mma_done[2]
@@ -127,8 +132,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // ---- A chunk: weight, split, store as K-major core matrices ----------
     const int c0 = kc * KC;
 #pragma unroll
-    for (int jj = 0; jj < 4; jj++) {
-      const int j = khalf * 4 + jj;  // k-core within the chunk
+    for (int jj = 0; jj < KC / 16; jj++) {
+      const int j = khalf * (KC / 16) + jj;  // k-core within the chunk
       float a[8];
 #pragma unroll
       for (int e = 0; e < 8; e++) {
@@ -186,31 +191,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   }
   ptx::tc_fence_after();
   if (ok) {
-    // ---- stage fp32 A rows for the band: As[k][m], c = b0 - KBAND + k ----
+    // ---- epilogue, per window of WC output columns: stage the fp32 A
+    // columns the window's band reads, As[k][m] with c = b0 + wc - KBAND + k,
+    // then TMEM rows + FP32 band -> filtered[n][v][b] ----------------------
     float* As = reinterpret_cast<float*>(smem);
-    constexpr int KW = BN + 2 * KBAND;
-    for (int k = khalf; k < KW; k += 2) {
-      const int c = b0 - KBAND + k;
-      float val = 0.f;
-      if (c >= 0 && c < nu) {
-        const size_t idx = (size_t)c * nv + v0 + m;
-        val = __ldg(P + idx) * __ldg(weights + idx);
-      }
-      As[k * 128 + m] = val;
-    }
-    __syncthreads();
-    // ---- epilogue: TMEM rows + FP32 band -> filtered[n][v][b] -------------
     const int q = warp & 3, h = warp >> 2;
     const int row = 32 * q + lane;
     float* orow = out + ((size_t)n * nv + v0 + row) * nu + b0;
 #pragma unroll 1
-    for (int cc = 0; cc < BN / 64; cc++) {
-      const int col0 = h * (BN / 2) + cc * 32;
+    for (int wc = 0; wc < BN; wc += WC) {
+      if (wc > 0) __syncthreads();  // every warp is done with the last window
+      for (int k = khalf; k < KW; k += 2) {
+        const int c = b0 + wc - KBAND + k;
+        float val = 0.f;
+        if (c >= 0 && c < nu) {
+          const size_t idx = (size_t)c * nv + v0 + m;
+          val = __ldg(P + idx) * __ldg(weights + idx);
+        }
+        As[k * 128 + m] = val;
+      }
+      __syncthreads();
+      const int col0 = wc + h * 32;  // this warp's 32 output columns
       float r[32];
       ptx::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, r);
       float win[32 + 2 * KBAND];
 #pragma unroll
-      for (int k = 0; k < 32 + 2 * KBAND; k++) win[k] = As[(col0 + k) * 128 + row];
+      for (int k = 0; k < 32 + 2 * KBAND; k++) win[k] = As[(h * 32 + k) * 128 + row];
 #pragma unroll
       for (int i = 0; i < 32; i++) {
         float acc = r[i];
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 size_t smem_for(int bn) {
   size_t stage = 2 * (128 * KC * 2) + 2 * ((size_t)bn * KC * 2);
-  size_t epi = (size_t)(bn + 2 * KBAND) * 128 * 4;
+  size_t epi = (size_t)(64 + 2 * KBAND) * 128 * 4;
   size_t main = 2 * stage;
   return (main > epi ? main : epi) + 64;
 }
@@ -282,7 +288,7 @@ void bf16x3_build_bsplit(int nu, const float* taps_half, uint16_t* out) {
 }
 
 bool bf16x3_supported(const FdkDev& d) {
-  if (d.nu % KC != 0 || d.nv % 128 != 0 || d.nu < 64) return false;
+  if (d.nu % 64 != 0 || d.nv % 128 != 0) return false;  // N tiles of 64, 128, 256 columns
   int dev = 0, major = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
