@@ -108,6 +108,26 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   const int khalf = tid >> 7;
   bool ok = true;
 
+  // This thread's A elements of a chunk (row m, columns c0 + 8 j + e of its
+  // KC/16 k-cores j), loaded one chunk ahead: the loads of chunk k + 1 are
+  // in flight while chunk k is split, its B copy waited for and its MMAs
+  // issued, instead of each chunk waiting a full L2 round trip.
+  constexpr int NE = KC / 2;
+  float pp[NE], pw[NE];
+  const float* Pm = P + v0 + m;
+  const float* Wm = weights + v0 + m;
+  auto load_chunk = [&](int kc) {
+#pragma unroll
+    for (int jj = 0; jj < KC / 16; jj++)
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const size_t c = (size_t)(kc * KC + 8 * (khalf * (KC / 16) + jj) + e);
+        pp[jj * 8 + e] = __ldg(Pm + c * nv);
+        pw[jj * 8 + e] = __ldg(Wm + c * nv);
+      }
+  };
+  load_chunk(0);
+
   for (int kc = 0; kc < nchunks && ok; kc++) {
     const int s = kc & 1;
     const uint32_t use = (uint32_t)(kc >> 1);
@@ -130,17 +150,12 @@ __global__ void __launch_bounds__(NTHREADS, 2)
       ptx::bulk_load(b_lo, src + BN * KC, B_BYTES, &bars[s]);
     }
     // ---- A chunk: weight, split, store as K-major core matrices ----------
-    const int c0 = kc * KC;
 #pragma unroll
     for (int jj = 0; jj < KC / 16; jj++) {
       const int j = khalf * (KC / 16) + jj;  // k-core within the chunk
       float a[8];
 #pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const int c = c0 + 8 * j + e;
-        const size_t idx = (size_t)c * nv + v0 + m;
-        a[e] = __ldg(P + idx) * __ldg(weights + idx);
-      }
+      for (int e = 0; e < 8; e++) a[e] = pp[jj * 8 + e] * pw[jj * 8 + e];
       uint32_t hi[4], lo[4];
 #pragma unroll
       for (int e = 0; e < 4; e++) {
@@ -158,6 +173,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
       *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
       *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
     }
+    if (kc + 1 < nchunks) load_chunk(kc + 1);
     ptx::fence_proxy_async_smem();
     bool w = ptx::mbar_wait(&bars[s], use & 1);  // B chunk landed
     if (!__syncthreads_and(w)) {
