@@ -132,12 +132,16 @@ void monte_fdk_geom_reference65(monte_fdk_geom* g);
 void monte_fdk_geom_reference325(monte_fdk_geom* g);
 
 /* Cosine weighting + ramp filter: proj[view][u][v] -> filtered[view][v][u].
- * recon/bp3d20.cpp:36-73. */
+ * recon/bp3d20.cpp:36-73.  With MONTE_MEM_HOST and both buffers pinned the
+ * views go up, through the filter and back down in overlapping ranges. */
 int monte_fdk_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
                      float* filtered, int filter_mode, int mem);
 /* Voxel-driven backprojection of filtered[view][v][u] into vol_xy[nz][ny][nx]
  * (overwritten; voxels outside the slab/mask are set to 0) and, if not NULL,
- * vol_zy[nx][ny][nz].  recon/bp3d20.cpp:81-166. */
+ * vol_zy[nx][ny][nz].  recon/bp3d20.cpp:81-166.  With MONTE_MEM_HOST,
+ * MONTE_BP_TILED, a full-width volume and pinned buffers, the views are
+ * uploaded in ranges under the backprojection of the earlier ranges, as in
+ * monte_fdk. */
 int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* filtered,
                           float* vol_xy, float* vol_zy, int bp_mode, int mem);
 /* Full FDK: filter then backproject.  `filtered` may be NULL (device scratch
@@ -150,8 +154,9 @@ int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* 
  * results equal the unpipelined path's bit for bit. */
 int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float* filtered,
               float* vol_xy, float* vol_zy, int filter_mode, int bp_mode, int mem);
-/* View ranges of the last monte_fdk call of this context that used host
- * memory: >= 1 when it ran pipelined, 0 when it ran unpipelined. */
+/* View ranges of the last host-memory monte_fdk, monte_fdk_filter or
+ * monte_fdk_backproject call of this context: >= 1 when it ran pipelined,
+ * 0 when it ran unpipelined. */
 int monte_fdk_last_host_ranges(const monte_ctx* ctx);
 
 /* Exact adjoint of monte_fdk_backproject (MONTE_BP_PLAIN coefficients): the

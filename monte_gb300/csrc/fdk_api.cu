@@ -347,19 +347,27 @@ int pipe_ranges(int n_views, int* r) {
   return nr;
 }
 
-int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
-                            float* filtered, float* dvol_xy, float* dvol_zy, int filter_mode,
-                            int variant) {
+// The stages a pipelined call runs.
+enum { kPipeFilter = 1, kPipeBackproject = 2 };
+
+// src: the host input, projections (kPipeFilter) or filtered projections
+// (backprojection alone); filtered: host output of the filter or null;
+// dvol_xy/dvol_zy: device addresses of the pinned host volumes.
+int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, int stages,
+                            const float* src, float* filtered, float* dvol_xy, float* dvol_zy,
+                            int filter_mode, int variant) {
+  const bool do_filter = (stages & kPipeFilter) != 0, do_bp = (stages & kPipeBackproject) != 0;
   const size_t view_elems = (size_t)g->nu * g->nv;
   const size_t pb = proj_bytes(g), vb = vol_bytes(g);
   int r[kPipeMaxRanges + 1];
   const int nr = pipe_ranges(g->n_views, r);
-  MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
+  if (do_filter) MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
   MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
-  if (nr > 1) MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "partial sums"));
-  float* dp = (float*)ctx->scratch[kScratchProj].ptr;
+  if (do_bp && nr > 1) MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "partial sums"));
+  float* dp = do_filter ? (float*)ctx->scratch[kScratchProj].ptr : nullptr;
   float* df = (float*)ctx->scratch[kScratchFiltered].ptr;
   float* dsum = (float*)ctx->scratch[kScratchVolXY].ptr;
+  float* din = do_filter ? dp : df;  // where the uploads land
   cudaEvent_t* ev = ctx->pipe_ev;
   // the copies start after the work already queued on the stream (which
   // may still read the staging buffers)
@@ -368,7 +376,7 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, const float
   MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvStart], 0));
   for (int i = 0; i < nr; i++) {
     const size_t off = (size_t)r[i] * view_elems;
-    MONTE_CUDA(ctx, cudaMemcpyAsync(dp + off, proj + off,
+    MONTE_CUDA(ctx, cudaMemcpyAsync(din + off, src + off,
                                     (size_t)(r[i + 1] - r[i]) * view_elems * sizeof(float),
                                     cudaMemcpyHostToDevice, ctx->copy_in));
     MONTE_CUDA(ctx, cudaEventRecord(ev[kEvIn + i], ctx->copy_in));
@@ -381,15 +389,18 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, const float
     const size_t off = (size_t)r[i] * view_elems;
     const size_t bytes = (size_t)(r[i + 1] - r[i]) * view_elems * sizeof(float);
     MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvIn + i], 0));
-    monte_fdk_geom gr = *g;  // the range's views as a scan of their own
-    gr.n_views = r[i + 1] - r[i];
-    MONTE_TRY(run_filter(ctx, &gr, dp + off, df + off, filter_mode));
-    if (filtered) {
-      MONTE_CUDA(ctx, cudaEventRecord(ev[kEvFilt + i], ctx->stream));
-      MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvFilt + i], 0));
-      MONTE_CUDA(ctx, cudaMemcpyAsync(filtered + off, df + off, bytes, cudaMemcpyDeviceToHost,
-                                      ctx->copy_out));
+    if (do_filter) {
+      monte_fdk_geom gr = *g;  // the range's views as a scan of their own
+      gr.n_views = r[i + 1] - r[i];
+      MONTE_TRY(run_filter(ctx, &gr, dp + off, df + off, filter_mode));
+      if (filtered) {
+        MONTE_CUDA(ctx, cudaEventRecord(ev[kEvFilt + i], ctx->stream));
+        MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvFilt + i], 0));
+        MONTE_CUDA(ctx, cudaMemcpyAsync(filtered + off, df + off, bytes, cudaMemcpyDeviceToHost,
+                                        ctx->copy_out));
+      }
     }
+    if (!do_bp) continue;
     // the backprojection ranges trail the filtered ones by a view: with
     // the flat-edge reads (MONTE_FDK_FLAT_EDGE) view k's last row and
     // column read on into view k + 1
@@ -403,7 +414,7 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, const float
     if (e != cudaSuccess) return cuda_fail(ctx, e, "backprojection launch");
     have_sum = true;
   }
-  ctx->last_bp_variant = variant;
+  if (do_bp) ctx->last_bp_variant = variant;
   ctx->last_host_ranges = nr;
   MONTE_CUDA(ctx, cudaEventRecord(ev[kEvOut], ctx->copy_out));
   MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvOut], 0));
@@ -411,25 +422,33 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, const float
   return MONTE_OK;
 }
 
-// Runs the pipelined path and returns 1 when the call qualifies for it:
-// tiled backprojection of full-width volumes, all host buffers pinned.
-// Returns 0 (nothing done) otherwise.
-int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
-                       float* filtered, float* vol_xy, float* vol_zy, int filter_mode, int bp_mode,
-                       int* rc) {
-  if (bp_mode != MONTE_BP_TILED || g->s_begin != 0 || g->s_end != g->nx) return 0;
-  if (filter_mode != MONTE_FILTER_FP32 && filter_mode != MONTE_FILTER_BF16X3) return 0;
-  const FdkDev d = make_fdk_dev(*g);
-  int variant = ctx->bp_tune_choice;
-  if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
-  if (!fdk_bp_tiled_supported(d, variant)) return 0;
-  float* mxy = (float*)host_mapped(vol_xy);
-  float* mzy = vol_zy ? (float*)host_mapped(vol_zy) : nullptr;
-  if (!mxy || (vol_zy && !mzy) || !host_mapped(proj) || (filtered && !host_mapped(filtered)))
+// Runs the pipelined path and returns 1 when the call qualifies for it, 0
+// (nothing done) otherwise.  It qualifies with every host buffer pinned,
+// and for the backprojection a tiled shape that fits and a full-width
+// volume.  stages as above; src: projections when filtering, else the
+// filtered projections.
+int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, int stages, const float* src,
+                       float* filtered, float* vol_xy, float* vol_zy, int filter_mode,
+                       int bp_mode, int* rc) {
+  const bool do_filter = (stages & kPipeFilter) != 0, do_bp = (stages & kPipeBackproject) != 0;
+  if (do_filter && filter_mode != MONTE_FILTER_FP32 && filter_mode != MONTE_FILTER_BF16X3)
     return 0;
+  if (!host_mapped(src) || (filtered && !host_mapped(filtered))) return 0;
+  int variant = -1;
+  float *mxy = nullptr, *mzy = nullptr;
+  if (do_bp) {
+    if (bp_mode != MONTE_BP_TILED || g->s_begin != 0 || g->s_end != g->nx) return 0;
+    const FdkDev d = make_fdk_dev(*g);
+    variant = ctx->bp_tune_choice;
+    if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
+    if (!fdk_bp_tiled_supported(d, variant)) return 0;
+    mxy = (float*)host_mapped(vol_xy);
+    mzy = vol_zy ? (float*)host_mapped(vol_zy) : nullptr;
+    if (!mxy || (vol_zy && !mzy)) return 0;
+  }
   *rc = pipe_init(ctx);
   if (*rc == MONTE_OK)
-    *rc = fdk_host_pipelined_body(ctx, g, proj, filtered, mxy, mzy, filter_mode, variant);
+    *rc = fdk_host_pipelined_body(ctx, g, stages, src, filtered, mxy, mzy, filter_mode, variant);
   if (*rc != MONTE_OK) {
     // nothing may still read or write the caller's buffers after the return
     cudaStreamSynchronize(ctx->copy_in);
@@ -489,6 +508,11 @@ int monte_fdk_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj,
   MONTE_TRY(enter(ctx));
   MONTE_TRY(prepare_tables(ctx, g));
   if (mem == MONTE_MEM_DEVICE) return run_filter(ctx, g, proj, filtered, filter_mode);
+  int rc = MONTE_OK;
+  ctx->last_host_ranges = 0;
+  if (fdk_host_pipelined(ctx, g, kPipeFilter, proj, filtered, nullptr, nullptr, filter_mode,
+                         MONTE_BP_TILED, &rc))
+    return rc;
   const size_t pb = proj_bytes(g);
   MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
   MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
@@ -511,6 +535,11 @@ int monte_fdk_backproject(monte_ctx* ctx, const monte_fdk_geom* g, const float* 
   MONTE_TRY(enter(ctx));
   MONTE_TRY(prepare_tables(ctx, g));
   if (mem == MONTE_MEM_DEVICE) return run_bp(ctx, g, filtered, vol_xy, vol_zy, bp_mode);
+  int rc = MONTE_OK;
+  ctx->last_host_ranges = 0;
+  if (fdk_host_pipelined(ctx, g, kPipeBackproject, filtered, nullptr, vol_xy, vol_zy,
+                         MONTE_FILTER_FP32, bp_mode, &rc))
+    return rc;
   const size_t pb = proj_bytes(g), vb = vol_bytes(g);
   MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
   MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "volume staging"));
@@ -547,7 +576,8 @@ int monte_fdk(monte_ctx* ctx, const monte_fdk_geom* g, const float* proj, float*
   }
   int rc = MONTE_OK;
   ctx->last_host_ranges = 0;
-  if (fdk_host_pipelined(ctx, g, proj, filtered, vol_xy, vol_zy, filter_mode, bp_mode, &rc))
+  if (fdk_host_pipelined(ctx, g, kPipeFilter | kPipeBackproject, proj, filtered, vol_xy, vol_zy,
+                         filter_mode, bp_mode, &rc))
     return rc;
   // pageable buffers, the plain backprojector or a column window: one
   // upload, the two stages, one download

@@ -86,3 +86,26 @@ def test_pageable_buffers_run_unpipelined(ctx):
     _, xyh, _ = _host(ctx, g, proj, abi.MONTE_FILTER_FP32, False, pinned=False)
     assert ctx.last_host_ranges() == 0
     assert np.array_equal(xyh, xyd)
+
+
+def test_pinned_filter_alone_equals_device_path(ctx):
+    g = _geom(180)
+    proj = fdk_projections(g.n_views, g.nu, g.nv, 12)
+    fd, _, _ = _device(ctx, g, proj, abi.MONTE_FILTER_FP32, False)
+    p = torch.from_numpy(proj).pin_memory()
+    fh = torch.full((g.n_views, g.nv, g.nu), float("nan"), pin_memory=True)
+    ctx.fdk_filter(g, p, fh, mode=abi.MONTE_FILTER_FP32)
+    assert ctx.last_host_ranges() == 3
+    assert np.array_equal(fh.numpy(), fd)
+
+
+def test_pinned_backprojection_alone_equals_device_path(ctx):
+    g = _geom(180, mask=20)
+    proj = fdk_projections(g.n_views, g.nu, g.nv, 13)
+    fd, xyd, zyd = _device(ctx, g, proj, abi.MONTE_FILTER_FP32, True)
+    f = torch.from_numpy(fd).pin_memory()
+    xy = torch.full((g.nz, g.ny, g.nx), float("nan"), pin_memory=True)
+    zy = torch.full((g.nx, g.ny, g.nz), float("nan"), pin_memory=True)
+    ctx.fdk_backproject(g, f, xy, vol_zy=zy, mode=abi.MONTE_BP_TILED)
+    assert ctx.last_host_ranges() == 3
+    assert np.array_equal(xy.numpy(), xyd) and np.array_equal(zy.numpy(), zyd)

@@ -141,3 +141,33 @@ def test_bad_arguments(ctx):
     g.sdd = 10.0  # detector inside the source distance
     with pytest.raises(MonteError):
         ctx.mc_run(g, dev, abi.mc_request(1, 1, (0, 1), (0, 64), (0, 64)), prim, prim.clone())
+
+
+def test_fan_beam_one_row_detector_replay(ctx):
+    """2-D (fan-beam) Monte Carlo with the same kernels.  The phantom is one
+    z-invariant slice of the cylinder phantom (one voxel 100 cm tall) and
+    the detector one row as tall, so every photon that reaches the detector
+    line is tallied whatever its height: the set-up of the reference's 2-D
+    programs (monte_cpp/c3_l.cpp: a 65x65 label image, a 65-bin detector row
+    per angle).  Seeded replay stays bit-exact with the CPU harness."""
+    lab, vox, org = phantoms.cylinder_inserts_labels()
+    x = golden("xcom")
+    sl = np.ascontiguousarray(lab[32:33])
+
+    def inputs(labels):
+        return abi.McInputs(labels, (vox, vox, 100.0), (org[0], org[1], -50.0),
+                            [-1, 0, 1, 1, 1], [0.0, 1.0, 1.2, 1.5, 1.9],
+                            [x["water"], x["ca"]], np.arange(20.0, 81.0), 80.0 - np.arange(20.0, 81.0))
+
+    host, dev = inputs(sl), inputs(torch.from_numpy(sl).cuda())
+    g = abi.mc_geom(60, 64, 1, 0.1, 50.0, 100.0, 3.5)
+    g.dv, g.half_v = 100.0, 50.0
+    req = abi.mc_request(4242, 64, (0, 6), (0, 64), (0, 1))
+    p_ref, s_ref, st_ref = oracle.mc_run(g, host, req)
+    assert p_ref.shape == (60, 64, 1) and p_ref.sum() > 0 and s_ref.sum() > 0
+    for kernel in (abi.MONTE_MC_PLAIN, abi.MONTE_MC_PERSISTENT):
+        req.kernel = kernel
+        p, s, st = _gpu_run(ctx, g, dev, req)
+        assert np.array_equal(p, p_ref), kernel
+        assert np.array_equal(s, s_ref), kernel
+        assert st["interactions"] == st_ref["interactions"]
