@@ -1,7 +1,8 @@
 /*
  * fdk_oracle.c -- CPU oracle for the FDK hot path.  TEST INFRASTRUCTURE:
  * only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
- * it, and only as the checker; the product never links or calls it.
+ * it, and only to check results or time the CPU form; the product never links
+ * or calls it.
  *
  * A restatement of recon/bp3d20.cpp and recon/bp3d20_325.cpp with their
  * hard-coded constants turned into monte_fdk_geom fields.  Two modes:
