@@ -212,3 +212,31 @@ def test_even_grid_backprojects_as_fast_as_odd(ctx):
         ctx.check_status()
         ms[n] = sorted(t)[1]
     assert ms[96] < 2.0 * ms[97], ms
+
+
+def test_volume_taller_than_the_field_of_view(ctx):
+    """A volume whose top and bottom slices project past the detector's
+    first and last rows: per view some voxel blocks lie inside the detector
+    (the per-lane edge tests are skipped for them), some straddle its row
+    edges (voxel-by-voxel classification, exact decisions near the edges)
+    and some project off it.  Every tile shape against the FP64 oracle."""
+    g = abi.fdk_geom_recon325(n_views=90, nu=128, nv=64, pitch_mm=3.2, n=65, voxel_mm=2.4)
+    proj = fdk_projections(g.n_views, g.nu, g.nv, 65)
+    v64 = oracle.fdk_backproject(g, oracle.fdk_filter(g, proj, precise=True))
+    _, ref = _run(ctx, g, proj, bp_mode=abi.MONTE_BP_PLAIN)
+    assert rel_rms(ref, v64) < 1e-5
+    v, ran = 0, 0
+    while True:
+        try:
+            ctx.set_bp_variant(v)
+        except MonteError:
+            break
+        _, got = _run(ctx, g, proj, bp_mode=abi.MONTE_BP_TILED)
+        ctx.check_status()
+        if ctx.last_bp_variant() == v:
+            ran += 1
+            assert rel_rms(got, v64) < 1e-5, v
+            assert rel_rms(got, ref) < 2e-6, v
+        v += 1
+    ctx.set_bp_variant(-1)
+    assert ran >= 12
