@@ -74,10 +74,12 @@ int fdk_validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid);
 // Time tiled backprojector shapes that fit g (`reps` launches each on the
 // context's stream, the first discarded) into scratch `dv` from filtered
 // projections `df`; *best = fastest shape, -1 if none fits.  candidates:
-// the shapes to time (NULL: all of them).
+// the shapes to time (NULL: all of them); padded: the padded copy of df
+// (launch_fdk_bp_tiled) or NULL.
 int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
                 const BpViewD* viewsd, const float* df, float* dv, int* best,
-                const int* candidates, int n_candidates, int reps);
+                const int* candidates, int n_candidates, int reps,
+                const float* padded = nullptr);
 // Shapes that led on the reference-size workloads, for quick tuning.
 extern const int kBpQuickCandidates[];
 extern const int kBpQuickCandidatesN;
@@ -107,11 +109,19 @@ struct BpPart {
   const float* acc_in;
 };
 // status: device int set to 1 if a bounded wait gave up (MONTE_ETIMEOUT);
-// part: NULL for all views from zero
+// part: NULL for all views from zero; padded: NULL, or a copy of filtered
+// with its rows padded to a multiple of 4 floats (fdk_bp_pad_rows), from
+// which the tiles are loaded when nu is not a multiple of 4 (a TMA row
+// stride must be a multiple of 16 bytes); the exact per-voxel path always
+// reads `filtered`.
 cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
                                 const float* filtered, float* vol_xy, float* vol_zy,
                                 int variant, int* status, cudaStream_t st,
-                                const BpPart* part = nullptr);
+                                const BpPart* part = nullptr, const float* padded = nullptr);
+// Row pitch (floats) of the padded copy, and the copy itself.
+inline int fdk_bp_pad_pitch(int nu) { return (nu + 3) & ~3; }
+cudaError_t launch_fdk_bp_pad_rows(const FdkDev& d, const float* filtered, float* padded,
+                                   cudaStream_t st);
 // Adjoints (fdk_adjoint.cu): forward projector = transpose of the plain
 // backprojector, into filtered-space layout [view][v][u] (vol_z: scratch of
 // the volume's size for its z-major copy); adjoint of the weighting +
@@ -122,7 +132,9 @@ cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, con
 cudaError_t launch_fdk_filter_adjoint(const FdkDev& d, const float* g, const float* weights,
                                       const float* taps_half, float* h, cudaStream_t st);
 int fdk_bp_tiled_variants();
-bool fdk_bp_tiled_supported(const FdkDev& d, int variant);
+// padded: the caller provides the padded copy of the filtered projections
+// (needed by the per-warp shapes when nu is not a multiple of 4)
+bool fdk_bp_tiled_supported(const FdkDev& d, int variant, bool padded = false);
 
 #ifdef __CUDACC__
 // Shared by the plain and tiled kernels: bilinear read of filtered[view]

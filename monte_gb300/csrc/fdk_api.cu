@@ -152,7 +152,7 @@ void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t) {
 
 int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
                 const BpViewD* viewsd, const float* df, float* dv, int* best,
-                const int* candidates, int n_candidates, int reps) {
+                const int* candidates, int n_candidates, int reps, const float* padded) {
   FdkDev d = make_fdk_dev(*g);
   if (reps < 2) reps = 2;
   cudaEvent_t e0, e1;
@@ -163,12 +163,12 @@ int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
   const int n = candidates ? n_candidates : fdk_bp_tiled_variants();
   for (int i = 0; i < n; i++) {
     const int v = candidates ? candidates[i] : i;
-    if (!fdk_bp_tiled_supported(d, v)) continue;
+    if (!fdk_bp_tiled_supported(d, v, padded != nullptr)) continue;
     float ms_min = 3.0e38f;
     for (int rep = 0; rep < reps; rep++) {
       cudaEventRecord(e0, ctx->stream);
       cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, dv, nullptr, v, ctx->d_status,
-                                          ctx->stream);
+                                          ctx->stream, nullptr, padded);
       cudaEventRecord(e1, ctx->stream);
       if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
         cudaEventDestroy(e0);
@@ -267,16 +267,27 @@ int run_bp(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_filtered, flo
     e = launch_fdk_bp_plain(d, views, viewsd, d_filtered, d_xy, d_zy, ctx->stream);
     ctx->last_bp_variant = -1;
   } else if (bp_mode == MONTE_BP_TILED) {
+    // rows that are not a multiple of 16 bytes: the tiles come from a
+    // padded copy (TMA row strides are multiples of 16 bytes)
+    const float* padded = nullptr;
+    if (d.nu % 4 != 0) {
+      const size_t pbytes = (size_t)g->n_views * g->nv * fdk_bp_pad_pitch(g->nu) * sizeof(float);
+      MONTE_TRY(ensure_slot(ctx, kScratchBpPad, pbytes, "padded filtered projections"));
+      padded = (const float*)ctx->scratch[kScratchBpPad].ptr;
+      cudaError_t ep = launch_fdk_bp_pad_rows(d, d_filtered, (float*)padded, ctx->stream);
+      if (ep != cudaSuccess) return cuda_fail(ctx, ep, "row padding launch");
+    }
+    const bool pad = padded != nullptr;
     int variant = ctx->bp_tune_choice;
-    if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
-    if (!fdk_bp_tiled_supported(d, variant)) {
+    if (variant < 0 || !fdk_bp_tiled_supported(d, variant, pad)) variant = 0;
+    if (!fdk_bp_tiled_supported(d, variant, pad)) {
       // the footprint of a voxel block does not fit a shared-memory box:
       // the one-voxel-per-thread kernel handles any geometry
       e = launch_fdk_bp_plain(d, views, viewsd, d_filtered, d_xy, d_zy, ctx->stream);
       ctx->last_bp_variant = -1;
     } else {
       e = launch_fdk_bp_tiled(d, views, viewsd, d_filtered, d_xy, d_zy, variant, ctx->d_status,
-                              ctx->stream);
+                              ctx->stream, nullptr, padded);
       ctx->last_bp_variant = variant;
     }
   } else {
@@ -434,6 +445,8 @@ int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, int stages, cons
   if (do_filter && filter_mode != MONTE_FILTER_FP32 && filter_mode != MONTE_FILTER_BF16X3)
     return 0;
   if (!host_mapped(src) || (filtered && !host_mapped(filtered))) return 0;
+  // rows that need a padded copy for the tiles take the unpipelined path
+  if (do_bp && g->nu % 4 != 0) return 0;
   int variant = -1;
   float *mxy = nullptr, *mzy = nullptr;
   if (do_bp) {
@@ -611,10 +624,17 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
   MONTE_CUDA(ctx, cudaMemsetAsync(ctx->scratch[kScratchFiltered].ptr, 0, pb, ctx->stream));
   const float* df = (const float*)ctx->scratch[kScratchFiltered].ptr;
   float* dv = (float*)ctx->scratch[kScratchVolXY].ptr;
+  const float* padded = nullptr;
+  if (g->nu % 4 != 0) {  // as run_bp: tiles from a copy with padded rows (zeros here)
+    const size_t pbytes = (size_t)g->n_views * g->nv * fdk_bp_pad_pitch(g->nu) * sizeof(float);
+    MONTE_TRY(ensure_slot(ctx, kScratchBpPad, pbytes, "autotune padded projections"));
+    MONTE_CUDA(ctx, cudaMemsetAsync(ctx->scratch[kScratchBpPad].ptr, 0, pbytes, ctx->stream));
+    padded = (const float*)ctx->scratch[kScratchBpPad].ptr;
+  }
   const BpView* views = (const BpView*)ctx->fdk_views.ptr;
   const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
   int pick = -1;
-  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick, nullptr, 0, 3));
+  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick, nullptr, 0, 3, padded));
   ctx->bp_tune_choice = pick;
   if (best) *best = pick;
   return monte_ctx_check_status(ctx);

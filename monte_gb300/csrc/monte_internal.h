@@ -72,6 +72,7 @@ enum ScratchSlot {
   kScratchAux3 = 10,
   kScratchStats = 11,
   kScratchFbp2 = 12,
+  kScratchBpPad = 13,  // filtered projections with rows padded to 16 bytes (TMA)
 };
 
 int set_error(monte_ctx* ctx, int code, const char* fmt, ...);

@@ -240,3 +240,31 @@ def test_volume_taller_than_the_field_of_view(ctx):
         v += 1
     ctx.set_bp_variant(-1)
     assert ran >= 12
+
+
+@pytest.mark.parametrize("nu", [130, 129])
+def test_detector_width_not_a_multiple_of_4(ctx, nu):
+    """Rows of nu floats are not a multiple of 16 bytes (as on the
+    reference's 65- and 325-wide detectors): the tiles come from a copy with
+    padded rows, the exact per-voxel path reads the original.  Every tile
+    shape, including the per-warp ones that need TMA, against the FP64
+    oracle."""
+    g = abi.fdk_geom_recon325(n_views=90, nu=nu, nv=96, pitch_mm=3.2, n=65, voxel_mm=1.6)
+    proj = fdk_projections(g.n_views, g.nu, g.nv, nu)
+    v64 = oracle.fdk_backproject(g, oracle.fdk_filter(g, proj, precise=True))
+    _, ref = _run(ctx, g, proj, bp_mode=abi.MONTE_BP_PLAIN)
+    v, ran = 0, 0
+    while True:
+        try:
+            ctx.set_bp_variant(v)
+        except MonteError:
+            break
+        _, got = _run(ctx, g, proj, bp_mode=abi.MONTE_BP_TILED)
+        ctx.check_status()
+        if ctx.last_bp_variant() == v:
+            ran += 1
+            assert rel_rms(got, v64) < 1e-5, v
+            assert rel_rms(got, ref) < 2e-6, v
+        v += 1
+    ctx.set_bp_variant(-1)
+    assert ran == v  # every shape ran, the per-warp ones on the padded copy
