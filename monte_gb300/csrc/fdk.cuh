@@ -124,11 +124,15 @@ cudaError_t launch_fdk_bp_pad_rows(const FdkDev& d, const float* filtered, float
                                    cudaStream_t st);
 // Adjoints (fdk_adjoint.cu): forward projector = transpose of the plain
 // backprojector, into filtered-space layout [view][v][u] (vol_z: scratch of
-// the volume's size for its z-major copy); adjoint of the weighting +
-// filter, [view][v][u] -> [view][u][v].
+// fdk_fp_scratch_bytes for the volume's z-major copy and its column
+// occupancy map); adjoint of the weighting + filter, [view][v][u] ->
+// [view][u][v].
 cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
                                        const float* vol, float* vol_z, float* out,
                                        cudaStream_t st);
+inline size_t fdk_fp_scratch_bytes(const monte_fdk_geom& g) {
+  return (size_t)g.nx * g.ny * g.nz * sizeof(float) + (size_t)g.nx * g.ny;
+}
 cudaError_t launch_fdk_filter_adjoint(const FdkDev& d, const float* g, const float* weights,
                                       const float* taps_half, float* h, cudaStream_t st);
 int fdk_bp_tiled_variants();

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
                                                         const BpViewD* __restrict__ viewsd,
                                                         const float* __restrict__ vol,
                                                         const float* __restrict__ vol_z,
+                                                        const unsigned char* __restrict__ occ,
                                                         float* __restrict__ out) {
   extern __shared__ float G[];  // [FP_COLS][nv]: column-major
   const int k = blockIdx.y;
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
     for (int q = lo; q <= hi; q++) {  // warp-uniform: one voxel column at a time
       const int s = x_major ? d.s_begin + m : q;
       const int t = x_major ? q : m;
+      if (!occ[(size_t)s * d.ny + t]) continue;  // an empty voxel column adds nothing
       const float X = fmaf((float)s, d.dvox, d.x0);
       const float Y = fmaf(-(float)t, d.dvox, d.y0);
       // the column's part of the coefficients, once; does it project near
@@ -93,12 +95,14 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
           int a = z - d.cz, b = t - d.ct, c = s - d.cs;
           if (a * a + b * b + c * c > d.mask_r2) continue;
         }
+        // an empty voxel contributes nothing: skip it before its
+        // coefficients (most voxels of a phantom in air are empty)
+        const float r = __ldg(src + z);
+        if (r == 0.f) continue;
         const float Z = fmaf(-(float)z, d.dvox, d.z0);
         int xi, yi;
         float fx, fy, w;
         if (!bp_coef_z(d, col, vd, s, t, z, Z, &xi, &yi, &fx, &fy, &w)) continue;
-        const float r = __ldg(src + z);
-        if (r == 0.f) continue;
         const float c = w * r * v.factor;
 #pragma unroll
         for (int dy = 0; dy < 2; dy++) {
@@ -122,6 +126,20 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
     int row = i / FP_COLS, cl = i % FP_COLS;
     if (cl < ncols) dst[(size_t)row * d.nu + c0 + cl] = G[cl * d.nv + row];
   }
+}
+
+// occ[s][t] = whether voxel column (s, t) of the z-major volume holds a
+// nonzero voxel (a warp per column)
+__global__ void column_occupancy_kernel(int ncols, int nz, const float* __restrict__ vol_z,
+                                        unsigned char* __restrict__ occ) {
+  const int col = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (col >= ncols) return;  // warp-uniform
+  const float* c = vol_z + (size_t)col * nz;
+  bool any = false;
+  for (int z = lane; z < nz && !any; z += 32) any = c[z] != 0.f;
+  any = __any_sync(0xffffffffu, any);
+  if (lane == 0) occ[col] = any ? 1 : 0;
 }
 
 // out[s][t][z] = in[z][t][s]: per t, a 32 x 32 tile of the (z, s) plane
@@ -207,11 +225,17 @@ cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, con
   transpose_zs_kernel<<<tg, dim3(32, 8), 0, st>>>(d.nx, d.ny, d.nz, vol, vol_z);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  unsigned char* occ = reinterpret_cast<unsigned char*>(vol_z + (size_t)d.nx * d.ny * d.nz);
+  const int ncols = d.nx * d.ny;
+  column_occupancy_kernel<<<(unsigned)((ncols * 32ull + 255) / 256), 256, 0, st>>>(ncols, d.nz,
+                                                                                 vol_z, occ);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
   size_t smem = (size_t)d.nv * FP_COLS * sizeof(float);
   e = cudaFuncSetAttribute(fp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   dim3 grid((d.nu + FP_COLS - 1) / FP_COLS, d.n_views);
-  fp_kernel<<<grid, FP_THREADS, smem, st>>>(d, views, viewsd, vol, vol_z, out);
+  fp_kernel<<<grid, FP_THREADS, smem, st>>>(d, views, viewsd, vol, vol_z, occ, out);
   return cudaGetLastError();
 }
 

@@ -669,7 +669,7 @@ int monte_fdk_forward_project(monte_ctx* ctx, const monte_fdk_geom* g, const flo
     dout = (float*)ctx->scratch[kScratchFiltered].ptr;
   }
   // z-major copy of the volume: the projector reads a voxel column along z
-  MONTE_TRY(ensure_slot(ctx, kScratchVolZY, vb, "z-major volume copy"));
+  MONTE_TRY(ensure_slot(ctx, kScratchVolZY, fdk_fp_scratch_bytes(*g), "z-major volume copy"));
   cudaError_t e = launch_fdk_forward_project(d, (const BpView*)ctx->fdk_views.ptr,
                                              (const BpViewD*)ctx->fdk_viewsd.ptr, dv,
                                              (float*)ctx->scratch[kScratchVolZY].ptr, dout,
@@ -708,7 +708,7 @@ int monte_fdk_backward(monte_ctx* ctx, const monte_fdk_geom* g, const float* gra
     dv = (const float*)ctx->scratch[kScratchVolXY].ptr;
     dout = (float*)ctx->scratch[kScratchProj].ptr;
   }
-  MONTE_TRY(ensure_slot(ctx, kScratchVolZY, vb, "z-major volume copy"));
+  MONTE_TRY(ensure_slot(ctx, kScratchVolZY, fdk_fp_scratch_bytes(*g), "z-major volume copy"));
   cudaError_t e = launch_fdk_forward_project(d, (const BpView*)ctx->fdk_views.ptr,
                                              (const BpViewD*)ctx->fdk_viewsd.ptr, dv,
                                              (float*)ctx->scratch[kScratchVolZY].ptr, tmp,
