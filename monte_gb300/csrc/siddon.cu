@@ -45,6 +45,20 @@ __device__ __forceinline__ bool ray_of(const SiddonDev& s, size_t r, int* view, 
   return true;
 }
 
+// Line integral of mu along the ray, the segments summed with Kahan's
+// compensation (the float sum of a few hundred terms otherwise loses ~1e-6).
+__device__ __forceinline__ float line_integral(const SiddonDev& s, const float* __restrict__ mu,
+                                               const float* o, const float* d) {
+  float sum = 0.f, comp = 0.f;
+  siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2], [&](size_t v, float len) {
+    const float y = __ldg(mu + v) * len - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+  });
+  return sum;
+}
+
 __global__ void siddon_forward_kernel(SiddonDev s, const float* __restrict__ mu,
                                       float* __restrict__ line, float* __restrict__ trans) {
   size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -53,10 +67,7 @@ __global__ void siddon_forward_kernel(SiddonDev s, const float* __restrict__ mu,
   if (!ray_of(s, r, &view, &iu, &iv, &cell)) return;
   float o[3], d[3];
   siddon_ray(s.P, s.V, s.U, s.W, view, iu, iv, o, d);
-  double Ld = 0.0;
-  siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-              [&](size_t v, double len) { Ld = fma((double)__ldg(mu + v), len, Ld); });
-  const float L = (float)Ld;
+  const float L = line_integral(s, mu, o, d);
   if (line) line[cell] = L;
   if (trans) trans[cell] = expf(-L);
 }
@@ -72,15 +83,10 @@ __global__ void siddon_backward_kernel(SiddonDev s, const float* __restrict__ mu
   float o[3], d[3];
   siddon_ray(s.P, s.V, s.U, s.W, view, iu, iv, o, d);
   float gL = grad_line ? grad_line[cell] : 0.0f;
-  if (grad_trans) {
-    double Ld = 0.0;
-    siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-                [&](size_t v, double len) { Ld = fma((double)__ldg(mu + v), len, Ld); });
-    gL -= grad_trans[cell] * expf(-(float)Ld);  // dT/dL = -T
-  }
+  if (grad_trans) gL -= grad_trans[cell] * expf(-line_integral(s, mu, o, d));  // dT/dL = -T
   if (gL == 0.0f) return;
   siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-              [&](size_t v, double len) { atomicAdd(grad_mu + v, gL * (float)len); });
+              [&](size_t v, float len) { atomicAdd(grad_mu + v, gL * len); });
 }
 
 int setup(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid, int vb, int ve,

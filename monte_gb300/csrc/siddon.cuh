@@ -21,18 +21,50 @@ struct SiddonGrid {
   double dx, dy, dz;       // voxel pitch (cm)
 };
 
+// Float-float numbers (value = hi + lo, |lo| <= ulp(hi) / 2) for the walk:
+// sums and products with their exact float errors (Knuth's two-sum, the
+// FMA two-product; T. J. Dekker, "A floating-point technique for extending
+// the available precision", Numer. Math. 18, 1971).  FP64 runs at a small
+// fraction of the FP32 rate on this GPU; these keep ~44 bits in FP32 work.
+struct SidFF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ SidFF sid_ff(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+
+// p * b + c for an integer-valued float p (a plane index, exact in float)
+__device__ __forceinline__ SidFF sid_ff_fma(float p, SidFF b, SidFF c) {
+  const float ph = p * b.hi;
+  const float pe = fmaf(p, b.hi, -ph);  // p * b.hi = ph + pe exactly
+  const float s = ph + c.hi;            // two-sum of ph and c.hi
+  const float bb = s - ph;
+  const float se = (ph - (s - bb)) + (c.hi - bb);
+  const float lo = se + pe + fmaf(p, b.lo, c.lo);
+  const float hi = s + lo;              // renormalise
+  return {hi, lo - (hi - s)};
+}
+
+__device__ __forceinline__ bool sid_le(SidFF a, SidFF b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo);
+}
+
 // Visit the voxels a ray o + t*d (|d| = 1, t in cm) crosses inside the
-// grid, calling f(voxel index, segment length in cm, as a double).
-// Crossing parameters are recomputed from integer plane indices at every
-// step, never accumulated.
+// grid, calling f(voxel index, segment length in cm).  Crossing parameters
+// are recomputed from integer plane indices at every step, never
+// accumulated.
 //
-// The walk runs in double.  Its parameters reach the ray's length inside the
-// grid (tens of cm) while segments are a fraction of a voxel, so in float
-// every segment length would carry an absolute error of ~1 ulp(t) -- about
-// 5e-5 of a 0.8 mm segment -- and the line integral of a ray crossing a few
-// strong boundaries would drift by more than 1e-5 relative.  The ray's entry
-// point (a small difference of large numbers: the source sits hundreds of
-// voxels from the grid) is likewise computed in double.
+// The parameters reach the ray's length (tens of cm) while segments are a
+// fraction of a voxel: in plain float every segment length would carry an
+// absolute error of ~1 ulp(t), about 5e-5 of a 0.8 mm segment, and a line
+// integral across a few strong boundaries would drift by more than 1e-5
+// relative.  So the per-ray set-up (the entry point, a small difference of
+// large numbers: the source sits hundreds of voxels from the grid) runs in
+// double, and the walk in float-float: a segment length, the difference of
+// two neighbouring crossings, is then exact to ~1e-13 cm before it is
+// rounded to float.
 template <typename F>
 __device__ __forceinline__ void siddon_walk(const SiddonGrid& g, float ox, float oy, float oz,
                                             float dx, float dy, float dz, F&& f) {
@@ -56,7 +88,7 @@ __device__ __forceinline__ void siddon_walk(const SiddonGrid& g, float ox, float
   // voxel at the entry: evaluate 1e-4 voxel inside the grid; crossing of
   // plane p along axis a at t = p * inv[a] + c[a]
   int idx[3], step[3];
-  double tnext[3], inv[3], c[3];
+  SidFF tnext[3], inv[3], c[3];
   const double dmax = fmax(fabs(dd[0]), fmax(fabs(dd[1]), fabs(dd[2])));
   const double tm = t0 + 1e-4 / dmax;
 #pragma unroll
@@ -66,28 +98,32 @@ __device__ __forceinline__ void siddon_walk(const SiddonGrid& g, float ox, float
     idx[a] = min(max(i, 0), n[a] - 1);
     step[a] = dd[a] > 0.0 ? 1 : -1;
     if (dd[a] == 0.0) {
-      inv[a] = 0.0;
-      c[a] = 0.0;
-      tnext[a] = 1.0e300;
+      inv[a] = {0.f, 0.f};
+      c[a] = {0.f, 0.f};
+      tnext[a] = {3.0e38f, 0.f};  // never
     } else {
-      inv[a] = 1.0 / dd[a];
-      c[a] = -od[a] * inv[a];
-      tnext[a] = fma((double)(idx[a] + (step[a] > 0 ? 1 : 0)), inv[a], c[a]);
+      const double ia = 1.0 / dd[a];
+      inv[a] = sid_ff(ia);
+      c[a] = sid_ff(-od[a] * ia);
+      tnext[a] = sid_ff_fma((float)(idx[a] + (step[a] > 0 ? 1 : 0)), inv[a], c[a]);
     }
   }
-  double t = t0;
+  SidFF t = sid_ff(t0);
+  const SidFF tend = sid_ff(t1);
   const int max_steps = g.nx + g.ny + g.nz + 3;
-  for (int it = 0; it < max_steps && t < t1; it++) {
-    int a = (tnext[0] <= tnext[1]) ? ((tnext[0] <= tnext[2]) ? 0 : 2) : ((tnext[1] <= tnext[2]) ? 1 : 2);
-    double tn = fmin(tnext[a], t1);
-    if (tn > t) {
-      size_t v = ((size_t)idx[2] * g.ny + idx[1]) * g.nx + idx[0];
-      f(v, tn - t);
+  for (int it = 0; it < max_steps && !sid_le(tend, t); it++) {
+    const int a = sid_le(tnext[0], tnext[1]) ? (sid_le(tnext[0], tnext[2]) ? 0 : 2)
+                                             : (sid_le(tnext[1], tnext[2]) ? 1 : 2);
+    const SidFF tn = sid_le(tnext[a], tend) ? tnext[a] : tend;
+    if (!sid_le(tn, t)) {
+      // neighbouring crossings: the difference of the high parts is exact
+      const float len = (tn.hi - t.hi) + (tn.lo - t.lo);
+      f(((size_t)idx[2] * g.ny + idx[1]) * g.nx + idx[0], len);
     }
     t = tn;
     idx[a] += step[a];
     if (idx[a] < 0 || idx[a] >= n[a]) break;
-    tnext[a] = fma((double)(idx[a] + (step[a] > 0 ? 1 : 0)), inv[a], c[a]);
+    tnext[a] = sid_ff_fma((float)(idx[a] + (step[a] > 0 ? 1 : 0)), inv[a], c[a]);
   }
 }
 
