@@ -56,7 +56,7 @@ def parse():
 
 WORKLOAD = "fdk: 360 views x 512(u) x 384(v) FP32 @0.8mm, SOD 500, SDD 1000 mm -> 325^3 FP32 @0.4mm"
 # measured DRAM traffic per backprojection launch of WORKLOAD, by tile shape
-BP_TRAFFIC = {29: 280.82e6 + 127.04e6, 24: 342.49e6 + 144.32e6, 26: 980.36e6 + 178.60e6,
+BP_TRAFFIC = {33: 280.64e6 + 127.57e6, 29: 280.82e6 + 127.04e6, 24: 342.49e6 + 144.32e6, 26: 980.36e6 + 178.60e6,
               16: 904.65e6 + 164.43e6}
 
 
