@@ -12,7 +12,7 @@ namespace monte {
 
 // Per-view constants of the backprojector, computed on the host in double
 // (recon/bp3d20.cpp:85-88,103-104,134-137,159) and rounded to float.
-struct BpView {
+struct alignas(16) BpView {  // 16-byte aligned: two vector loads per view
   float c, s;     // cos, sin of the view angle
   float px, py;   // rotated source position
   float tanb;     // tan() as the distance term evaluates it
