@@ -118,10 +118,11 @@ cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpVi
                                 const float* filtered, float* vol_xy, float* vol_zy,
                                 int variant, int* status, cudaStream_t st,
                                 const BpPart* part = nullptr, const float* padded = nullptr);
-// Row pitch (floats) of the padded copy, and the copy itself.
+// Row pitch (floats) of the padded copy, and the copy itself, of views
+// [k_begin, k_end) (k_end < 0: to the last view).
 inline int fdk_bp_pad_pitch(int nu) { return (nu + 3) & ~3; }
 cudaError_t launch_fdk_bp_pad_rows(const FdkDev& d, const float* filtered, float* padded,
-                                   cudaStream_t st);
+                                   cudaStream_t st, int k_begin = 0, int k_end = -1);
 // Adjoints (fdk_adjoint.cu): forward projector = transpose of the plain
 // backprojector, into filtered-space layout [view][v][u] (vol_z: scratch of
 // fdk_fp_scratch_bytes for the volume's z-major copy and its column

@@ -375,6 +375,14 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, int stages,
   if (do_filter) MONTE_TRY(ensure_slot(ctx, kScratchProj, pb, "projection staging"));
   MONTE_TRY(ensure_slot(ctx, kScratchFiltered, pb, "filtered staging"));
   if (do_bp && nr > 1) MONTE_TRY(ensure_slot(ctx, kScratchVolXY, vb, "partial sums"));
+  // rows that are not a multiple of 16 bytes: every backprojection range
+  // first copies its views into the padded layout its tiles load from
+  float* padded = nullptr;
+  if (do_bp && g->nu % 4 != 0) {
+    const size_t pbytes = (size_t)g->n_views * g->nv * fdk_bp_pad_pitch(g->nu) * sizeof(float);
+    MONTE_TRY(ensure_slot(ctx, kScratchBpPad, pbytes, "padded filtered projections"));
+    padded = (float*)ctx->scratch[kScratchBpPad].ptr;
+  }
   float* dp = do_filter ? (float*)ctx->scratch[kScratchProj].ptr : nullptr;
   float* df = (float*)ctx->scratch[kScratchFiltered].ptr;
   float* dsum = (float*)ctx->scratch[kScratchVolXY].ptr;
@@ -419,9 +427,13 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, int stages,
     const int kb = i == 0 ? 0 : r[i] - 1, ke = last ? g->n_views : r[i + 1] - 1;
     if (ke == kb && !last) continue;
     const BpPart part{kb, ke, have_sum ? dsum : nullptr};
+    if (padded) {
+      cudaError_t ep = launch_fdk_bp_pad_rows(d, df, padded, ctx->stream, kb, ke);
+      if (ep != cudaSuccess) return cuda_fail(ctx, ep, "row padding launch");
+    }
     cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, last ? dvol_xy : dsum,
                                         last ? dvol_zy : nullptr, variant, ctx->d_status,
-                                        ctx->stream, &part);
+                                        ctx->stream, &part, padded);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "backprojection launch");
     have_sum = true;
   }
@@ -445,16 +457,15 @@ int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, int stages, cons
   if (do_filter && filter_mode != MONTE_FILTER_FP32 && filter_mode != MONTE_FILTER_BF16X3)
     return 0;
   if (!host_mapped(src) || (filtered && !host_mapped(filtered))) return 0;
-  // rows that need a padded copy for the tiles take the unpipelined path
-  if (do_bp && g->nu % 4 != 0) return 0;
   int variant = -1;
   float *mxy = nullptr, *mzy = nullptr;
   if (do_bp) {
     if (bp_mode != MONTE_BP_TILED || g->s_begin != 0 || g->s_end != g->nx) return 0;
     const FdkDev d = make_fdk_dev(*g);
+    const bool pad = g->nu % 4 != 0;  // tiles from a padded copy
     variant = ctx->bp_tune_choice;
-    if (variant < 0 || !fdk_bp_tiled_supported(d, variant)) variant = 0;
-    if (!fdk_bp_tiled_supported(d, variant)) return 0;
+    if (variant < 0 || !fdk_bp_tiled_supported(d, variant, pad)) variant = 0;
+    if (!fdk_bp_tiled_supported(d, variant, pad)) return 0;
     mxy = (float*)host_mapped(vol_xy);
     mzy = vol_zy ? (float*)host_mapped(vol_zy) : nullptr;
     if (!mxy || (vol_zy && !mzy)) return 0;

@@ -79,6 +79,31 @@ def test_pipeline_with_tensor_core_filter(ctx):
     assert np.array_equal(fh, fd) and np.array_equal(xyh, xyd)
 
 
+@pytest.mark.parametrize("nu", [129, 126])
+def test_pipeline_with_odd_detector_widths(ctx, nu):
+    """widths whose rows are not a multiple of 16 bytes: each range pads its
+    views' rows before its backprojection (the tiles load from the padded
+    copy, the exact per-voxel path reads the filtered views themselves)"""
+    g = abi.fdk_geom_recon325(n_views=120, nu=nu, nv=96, pitch_mm=3.2, n=49, voxel_mm=2.4)
+    proj = fdk_projections(g.n_views, g.nu, g.nv, 40 + nu)
+    try:
+        for variant in (33, 0):
+            ctx.set_bp_variant(variant)
+            fd, xyd, zyd = _device(ctx, g, proj, abi.MONTE_FILTER_FP32, True)
+            assert ctx.last_bp_variant() == variant
+            fh, xyh, zyh = _host(ctx, g, proj, abi.MONTE_FILTER_FP32, True)
+            assert ctx.last_host_ranges() == 3 and ctx.last_bp_variant() == variant
+            assert np.array_equal(fh, fd) and np.array_equal(xyh, xyd) and np.array_equal(zyh, zyd)
+            # the backprojection alone, from pinned filtered projections
+            f = torch.from_numpy(fd).pin_memory()
+            xy = torch.full((g.nz, g.ny, g.nx), float("nan"), pin_memory=True)
+            ctx.fdk_backproject(g, f, xy, mode=abi.MONTE_BP_TILED)
+            assert ctx.last_host_ranges() == 3
+            assert np.array_equal(xy.numpy(), xyd)
+    finally:
+        ctx.set_bp_variant(-1)
+
+
 def test_pageable_buffers_run_unpipelined(ctx):
     g = _geom(24)
     proj = fdk_projections(g.n_views, g.nu, g.nv, 3)
