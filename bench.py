@@ -314,6 +314,13 @@ def batch_bench(ctx, device, scale):
 
     for name, mode, opts, warm in (("fused", abi.MONTE_BATCH_FUSED, abi.MONTE_BATCH_AUTOTUNE, 1),
                                    ("sequential", abi.MONTE_BATCH_SEQUENTIAL, 0, 0)):
+        # the fused form transports against local majorants; the sequential
+        # one-instance form keeps the reference's single majorant
+        for j in b.jobs:
+            if mode == abi.MONTE_BATCH_FUSED:
+                j.mc.flags |= abi.MONTE_MC_LOCAL_MAJORANT
+            else:
+                j.mc.flags &= ~abi.MONTE_MC_LOCAL_MAJORANT
         t0 = time.time()
         plan = ctx.batch(b.xcom, b.jobs, mode=mode, options=opts)
         torch.cuda.synchronize(device)

@@ -187,6 +187,14 @@ int monte_fdk_set_bp_variant(monte_ctx* ctx, int variant);
 /* Which kernel the last monte_fdk_backproject/monte_fdk call of this context
  * ran: a tile shape index >= 0, or -1 for MONTE_BP_PLAIN. */
 int monte_fdk_last_bp_variant(const monte_ctx* ctx);
+/* How often the tiled backprojectors left FP32 since the last reset:
+ * counts[0] = voxel-view pairs decided in double next to a discontinuity
+ * of the reference operator (the detector edges, recon/bp3d20.cpp:116,152),
+ * counts[1] = (voxel column, view) pairs whose distance-weight sign was
+ * taken in double (tmp_s near 0, :140).  Waits for the context's stream;
+ * reset != 0 zeroes the counters.  No counterpart in the reference: it
+ * bounds the double-precision share of a run. */
+int monte_fdk_exact_counts(monte_ctx* ctx, uint64_t* counts, int reset);
 /* Check the context's status word: MONTE_ETIMEOUT if a bounded wait inside
  * a kernel gave up since the last check (the word is then cleared).
  * Synchronizes the context's stream. */
@@ -246,6 +254,16 @@ int monte_fbp2(monte_ctx* ctx, const monte_fbp2_geom* g, const float* proj, floa
                                           (monte_cpp/CBCT_real2.cpp:193,460-463) */
 #define MONTE_MC_NO_RAYLEIGH_TALLY 0x4 /* photons whose last interaction was Rayleigh
                                           are not tallied (monte_cpp/CBCT_real2.cpp:373-397) */
+/* Transport switch (not a reference behaviour): delta tracking against
+ * majorants local to macro cells of the phantom (the largest attenuation
+ * among the labels of a cell and its 26 neighbours) instead of the
+ * reference's single majorant over the whole phantom
+ * (monte_cu/CBCT_real325im.cu:866-868).  Exact in distribution -- the
+ * same tallies in expectation -- but the random numbers are used
+ * differently, so histories differ from those without the flag.  Far fewer
+ * virtual collisions where soft tissue or air neighbours bone.  Not
+ * supported by monte_mc_run_noalloc. */
+#define MONTE_MC_LOCAL_MAJORANT    0x8
 
 /* Kernels. */
 #define MONTE_MC_PLAIN      0 /* one thread per emitting pixel, histories in sequence
@@ -337,6 +355,10 @@ typedef struct monte_mc_stats {
   uint64_t primary_counts;  /* tallied */
   uint64_t scatter_counts;  /* tallied */
   uint64_t dropped;         /* histories stopped by a step or rejection cap */
+  uint64_t rayleigh;        /* interactions by kind: coherent (no deflection), */
+  uint64_t compton;         /* incoherent (Klein-Nishina), */
+  uint64_t photoelectric;   /* photo-absorption */
+  uint64_t majorant_legs;   /* moves of one macro-cell leg (MONTE_MC_LOCAL_MAJORANT) */
 } monte_mc_stats;
 
 /* Defaults equal to monte_cu/CBCT_real325im.cu: 360 views, 325x325 pixels
@@ -351,6 +373,35 @@ void monte_mc_geom_reference_cpu(monte_mc_geom* g);
  * tolerated) into four [201] arrays indexed by keV.  Host only, no GPU. */
 int monte_xcom_parse_csv(const char* text, size_t len, float* coherent, float* incoherent,
                          float* photoelectric, float* total);
+
+/* The reference's source spectrum as lines (monte_cu/CBCT_real325.cu:
+ * 349-389 reads the table, :479-486 samples it): cum[0..n_bins] is a
+ * cumulative table over half-keV bins (250 bins in 125kv_al2mm.txt /
+ * 125kv_al10mm.txt); a uniform u in (0, 1] selects the first bin d with
+ * cum[d] <= u <= cum[d+1], energy (d + 1) * bin_kev, and falls back to
+ * fallback_kev when no bin holds it (the reference's start_keV, 140).
+ * Writes the n_bins + 1 lines (bin energies, then the fallback) with the
+ * probability of each under that rule -- the reference's distribution
+ * exactly, whatever the table (an all-zero table, what the reference's
+ * reader leaves at :384, gives the fallback alone) -- for monte_spectrum.
+ * energy_kev and weight hold n_bins + 1 doubles.  Host only, no GPU. */
+int monte_spectrum_from_cumulative(const float* cum, int32_t n_bins, double bin_kev,
+                                   double fallback_kev, double* energy_kev, double* weight,
+                                   int32_t* n_lines);
+
+/* Whitespace-separated numbers of a text table (the reference's fscanf
+ * "%f" reads of 125kv_al*.txt, CBCT_real325.cu:363-386) into values;
+ * *n_values = how many were read (at most max_values).  Host only. */
+int monte_parse_numbers(const char* text, size_t len, float* values, int32_t max_values,
+                        int32_t* n_values);
+
+/* Draw the source energies of histories 0..n-1 of stream (seed, job) with
+ * the Monte Carlo kernels' own sampler (the first draw of every history of
+ * monte_mc_run, an alias table over the lines), into energies[n] (float
+ * keV, following `mem`).  No counterpart in the reference: it shows the
+ * sampled spectrum without running transport. */
+int monte_mc_sample_energies(monte_ctx* ctx, const monte_spectrum* spec, uint64_t seed,
+                             uint32_t job, uint64_t n, float* energies, int mem);
 
 /* Run the Monte Carlo.  primary and scatter are int64 [n_views][nu][nv]
  * tallies that the call ADDS to (zero them first); they follow `mem`.
@@ -373,14 +424,21 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
  * static device array of about 280 KB that every GPU loading the library
  * holds until exit.  Same semantics as monte_mc_run with the persistent or
  * plain kernel, on the current device and `cuda_stream` (NULL: the legacy
- * default stream); labels, primary and scatter must be device pointers.
- * Requests with more than MONTE_NOALLOC_MAX_VIEWS views or
- * MONTE_NOALLOC_MAX_PIXELS pixels along an axis are rejected (MONTE_EINVAL).
- * The first call on a device looks up the array's address
- * (cudaGetSymbolAddress); make it before any stream capture.  All calls on a
- * device share the array, which keeps the last call's contents: calls whose
- * work overlaps on the GPU race and must be serialized.  If stats is not
- * NULL the call waits for the stream.  Errors: monte_last_error(NULL). */
+ * default stream); labels, primary and scatter must be device (or managed)
+ * memory, else MONTE_EINVAL.  Requests with more than
+ * MONTE_NOALLOC_MAX_VIEWS views or MONTE_NOALLOC_MAX_PIXELS pixels along an
+ * axis are rejected (MONTE_EINVAL), and so is MONTE_MC_LOCAL_MAJORANT
+ * (MONTE_EUNSUPPORTED: its per-phantom tables do not fit the array).  The
+ * first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) and keeps it for the process's life: do not
+ * cudaDeviceReset a device between calls.  The call cannot be captured into
+ * a CUDA graph (its tables go up from host staging the next call reuses):
+ * on a capturing stream it returns MONTE_EUNSUPPORTED and issues nothing.
+ * All calls on a device share the array, which keeps the last call's
+ * contents: calls whose work overlaps on the GPU race and must be
+ * serialized; calls queued one after another on one stream are fine.  If
+ * stats is not NULL the call waits for the stream.  Errors:
+ * monte_last_error(NULL). */
 int monte_mc_run_noalloc(const monte_mc_geom* g, const monte_mc_phantom* ph,
                          const monte_xcom* xcom, const monte_spectrum* spec,
                          const monte_mc_request* run, int64_t* primary, int64_t* scatter,

@@ -97,6 +97,7 @@ def fdk_geom_reference325():
 MONTE_MC_STALE_SIN_PHI = 0x1
 MONTE_MC_FIRST_COMPTON_Z = 0x2
 MONTE_MC_NO_RAYLEIGH_TALLY = 0x4
+MONTE_MC_LOCAL_MAJORANT = 0x8
 class Fbp2Geom(C.Structure):
     """monte_fbp2_geom."""
 
@@ -219,7 +220,9 @@ class McStats(C.Structure):
     """monte_mc_stats."""
 
     _fields_ = [(n, C.c_uint64) for n in ("histories", "woodcock_steps", "interactions",
-                                          "primary_counts", "scatter_counts", "dropped")]
+                                          "primary_counts", "scatter_counts", "dropped",
+                                          "rayleigh", "compton", "photoelectric",
+                                          "majorant_legs")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

@@ -47,6 +47,7 @@ struct BatchJob {
   size_t o_tables = 0, o_views = 0, o_pixels = 0;
   size_t o_bpv = 0, o_bpvd = 0, o_weights = 0, o_taps = 0, o_bsplit = 0;
   size_t o_filtered = 0, o_map = 0;
+  size_t o_local = 0;            // local-majorant tables + class grid (MONTE_MC_LOCAL_MAJORANT)
   // device pointers
   const BpView* bpv = nullptr;
   const BpViewD* bpvd = nullptr;
@@ -67,7 +68,7 @@ struct monte_batch {
   monte::DevBuf arena;
   size_t o_mcdev = 0, o_starts = 0, o_counters = 0;
   unsigned long long total = 0;
-  unsigned long long* counters = nullptr;  // [0] batch counter, [8..15] stats, [16+j] per job
+  unsigned long long* counters = nullptr;  // [0] batch counter, [4..13] stats, [16+j] per job
   cudaStream_t lanes[monte::kLanes] = {};
   cudaEvent_t fork = nullptr;
   cudaEvent_t join[monte::kLanes] = {};
@@ -183,7 +184,7 @@ int capture(monte_batch* B) {
     unsigned char* base = (unsigned char*)B->arena.ptr;
     e = launch_mc_batch((const McDev*)(base + B->o_mcdev),
                         (const unsigned long long*)(base + B->o_starts), n, B->total, B->counters,
-                        B->counters + 8, ctx->sm_count, s0);
+                        B->counters + 4, ctx->sm_count, s0);
     if (e != cudaSuccess) return fail(cuda_fail(ctx, e, "batch Monte Carlo launch"));
   }
   e = cudaEventRecord(B->fork, s0);
@@ -249,6 +250,9 @@ int create_plan(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* j
     b.o_taps = take(ft[j].taps.size() * 4);
     b.o_bsplit = take(ft[j].bsplit.size() * 2);
     b.o_filtered = take(b.ncell * 4);
+    if (J.mc.flags & MONTE_MC_LOCAL_MAJORANT)
+      b.o_local = take(sizeof(mc_local_tables) +
+                       (size_t)b.mc.P.mgx * b.mc.P.mgy * b.mc.P.mgz * sizeof(uint16_t));
     b.o_map = J.map ? 0 : take(b.ncell * 4);
     b.filter_mode = (mode == MONTE_BATCH_FUSED && !ft[j].bsplit.empty()) ? MONTE_FILTER_BF16X3
                                                                            : MONTE_FILTER_FP32;
@@ -281,6 +285,15 @@ int create_plan(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* j
     MONTE_TRY(upload(ctx, ft[j].weights.data(), base + b.o_weights, ft[j].weights.size() * 4));
     MONTE_TRY(upload(ctx, ft[j].taps.data(), base + b.o_taps, ft[j].taps.size() * 4));
     MONTE_TRY(upload(ctx, ft[j].bsplit.data(), base + b.o_bsplit, ft[j].bsplit.size() * 2));
+    std::vector<mc_local_tables> Lt;
+    std::vector<uint16_t> cls;
+    if (J.mc.flags & MONTE_MC_LOCAL_MAJORANT) {
+      Lt.resize(1);
+      MONTE_TRY(mc_build_macro(ctx, &J.phantom, xcom, true, b.mc.P, Lt.data(), &cls, nullptr));
+      MONTE_TRY(upload(ctx, Lt.data(), base + b.o_local, sizeof(mc_local_tables)));
+      MONTE_TRY(upload(ctx, cls.data(), base + b.o_local + sizeof(mc_local_tables),
+                       cls.size() * sizeof(uint16_t)));
+    }
     // the uploads read host vectors that die at the end of this iteration
     MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     b.bpv = (const BpView*)(base + b.o_bpv);
@@ -296,9 +309,13 @@ int create_plan(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* j
     d.U = (const mc_pixel*)(base + b.o_pixels);
     d.W = d.U + J.mc.nu;
     d.labels = J.phantom.labels;
+    if (J.mc.flags & MONTE_MC_LOCAL_MAJORANT) {
+      d.L = (const mc_local_tables*)(base + b.o_local);
+      d.mclass = (const uint16_t*)(base + b.o_local + sizeof(mc_local_tables));
+    }
     d.prim = (unsigned long long*)J.primary;
     d.scat = (unsigned long long*)J.scatter;
-    d.stats = B->counters + 8;
+    d.stats = B->counters + 4;
     d.counter = B->counters + 16 + j;
     d.total = b.histories;
     devs[j] = d;
@@ -411,15 +428,10 @@ int monte_batch_stats(monte_batch* B, monte_mc_stats* stats) {
   monte_ctx* ctx = B->ctx;
   if (!stats) return set_error(ctx, MONTE_EINVAL, "null stats");
   MONTE_TRY(enter(ctx));
-  unsigned long long h[8];
-  MONTE_CUDA(ctx, cudaMemcpyAsync(h, B->counters + 8, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  unsigned long long h[kMcStats];
+  MONTE_CUDA(ctx, cudaMemcpyAsync(h, B->counters + 4, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  stats->histories = h[0];
-  stats->woodcock_steps = h[1];
-  stats->interactions = h[2];
-  stats->primary_counts = h[3];
-  stats->scatter_counts = h[4];
-  stats->dropped = h[5];
+  mc_stats_from(h, stats);
   return MONTE_OK;
 }
 

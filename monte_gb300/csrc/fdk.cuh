@@ -12,12 +12,27 @@ namespace monte {
 
 // Per-view constants of the backprojector, computed on the host in double
 // (recon/bp3d20.cpp:85-88,103-104,134-137,159) and rounded to float.
-struct alignas(16) BpView {  // 16-byte aligned: two vector loads per view
+//
+// The detector coordinates of voxel column (s, t) in this view follow from
+// two affine functions of the voxel indices,
+//   Vx = A + s B + t C   (distance from the source along the central ray)
+//   W  = D + s E + t F   (K Vy with K = sdd / du, Vy across the central ray)
+// as y = half_u / du - W / Vx and x(z) = half_v / dv - (sdd / dv) Z(z) / Vx.
+// Each coefficient is split into an exact part (suffix h: a multiple of one
+// power of two per view and function, chosen so that the h-sum is exact in
+// float for every voxel of the grid) and a small remainder (suffix l).  The
+// kernels thus evaluate Vx and W to ~1e-12 relative in a few FMAs, and the
+// coordinates to ~1e-8 pixel, where float arithmetic on the rotated voxel
+// position alone leaves ~1e-5 pixel (the reference works in double).
+struct alignas(16) BpView {  // 80 bytes: five vector loads per view
+  float ah, bh, ch, al;
+  float bl, cl, dh, eh;
+  float fh, dl, el, fl;
   float c, s;     // cos, sin of the view angle
-  float px, py;   // rotated source position
   float tanb;     // tan() as the distance term evaluates it
   float rs;       // 1/sqrt(1+tanb^2)
   float factor;   // dbeta * scale * scale2
+  float px, py;   // rotated source position
   float pad;
 };
 
@@ -48,6 +63,12 @@ struct FdkDev {
   float inv_du_lo, inv_dv_lo;
   float dvox_inv_dv, dvox_inv_dv_lo;
   float xmax, ymax;      // accepted detector coordinate ranges [0,xmax], [0,ymax]
+  // float pairs (hi + lo) of the constants of the exact coordinate path
+  // (BpView): yc = half_u / du, xc = half_v / dv, kv = sdd / dv,
+  // kb = sdd * dvox / dv (dx/dz times Vx), and z0, dvox
+  float yc_h, yc_l, xc_h, xc_l;
+  float kv_h, kv_l, kb_h, kb_l;
+  float z0_h, z0_l, dz_h, dz_l;
 };
 
 // (h - p) / pitch as (h - p) * (inv_hi + inv_lo), the product rounded once.
@@ -108,6 +129,11 @@ struct BpPart {
   int k_begin, k_end;
   const float* acc_in;
 };
+// Counters after the status word (ints kBpExactSlot.. of the context's
+// status array, two uint64): voxel-view pairs the tiled backprojectors
+// decided in double (bp_ref_voxel) and (column, view) pairs whose distance
+// weight's sign was taken in double (bp_ts_negative).
+constexpr int kBpExactSlot = 8;
 // status: device int set to 1 if a bounded wait gave up (MONTE_ETIMEOUT);
 // part: NULL for all views from zero; padded: NULL, or a copy of filtered
 // with its rows padded to a multiple of 4 floats (fdk_bp_pad_rows), from
@@ -229,14 +255,102 @@ __device__ __forceinline__ void bp_view_frame(const FdkDev& d, const BpView& v, 
   *Vy = fmaf(Y, v.c, -(X * v.s));
 }
 
+// ---- exact detector coordinates (float pairs) ---------------------------
+
+// An unevaluated sum h + l of two floats.
+struct Fpair {
+  float h, l;
+};
+
+// 1/v: the hardware approximation refined by one Newton-Raphson step,
+// r + r (1 - v r), within an ulp of the correctly rounded reciprocal (v is
+// a normal number here: a source distance or a squared weight distance).
+__device__ __forceinline__ float rcp_nr(float v) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return fmaf(r, fmaf(-v, r, 1.0f), r);
+}
+
+// The pair arithmetic below relies on every product and sum being rounded
+// on its own (the error terms recover exactly what that rounding lost), so
+// it is written with the _rn intrinsics, which the compiler never fuses,
+// whatever -fmad says for the file that includes it.
+
+// a * b for pairs, to ~2^-46 relative (the l * l term dropped).
+__device__ __forceinline__ Fpair bp_mul(Fpair a, Fpair b) {
+  const float p = __fmul_rn(a.h, b.h);
+  return {p, fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)))};
+}
+
+// c - p for pairs with |c.h| >= |p.h| (Dekker's fast two-sum on the high
+// parts: their difference's rounding error is recovered exactly), then
+// normalised so that h is the sum rounded to float and |l| <= ulp(h) / 2.
+// The low parts of products (bp_mul) carry the affine remainders, up to
+// ~1e-4 of the value; without the normalisation, floor(h) could miss the
+// coordinate's integer part by one near an integer.
+__device__ __forceinline__ Fpair bp_sub(Fpair c, Fpair p) {
+  const float h = __fsub_rn(c.h, p.h);
+  const float l = __fadd_rn(__fsub_rn(__fsub_rn(c.h, h), p.h), __fsub_rn(c.l, p.l));
+  const float s = __fadd_rn(h, l);
+  return {s, __fsub_rn(l, __fsub_rn(s, h))};
+}
+
+// 1 / (vh + vl) for |vl| << |vh|: vh's reciprocal, its exact residual
+// e = 1 - vh rh, and the series rh (1 + e - q + q^2) with q = vl rh.
+__device__ __forceinline__ Fpair bp_recip(float vh, float vl) {
+  const float rh = rcp_nr(vh);
+  const float e = fmaf(-vh, rh, 1.0f);
+  const float q = __fmul_rn(vl, rh);
+  return {rh, __fmul_rn(rh, fmaf(q, q, __fsub_rn(e, q)))};
+}
+
+// (sdd / dv) Z(z) with Z(z) = z0 - z dvox, as a pair: the z term of every
+// detector row coordinate, x(z) = half_v / dv - bp_zterm(z) / Vx.
+__device__ __forceinline__ Fpair bp_zterm(const FdkDev& d, int z) {
+  const float zf = (float)z;
+  const float p = __fmul_rn(zf, d.dz_h);
+  const float pe = fmaf(zf, d.dz_h, -p);  // z dz_h = p + pe exactly
+  const float h = __fsub_rn(d.z0_h, p);   // two-sum of z0_h and -p
+  const float bb = __fsub_rn(h, d.z0_h);
+  const float e = __fadd_rn(__fsub_rn(d.z0_h, __fsub_rn(h, bb)), __fsub_rn(-p, bb));
+  const Fpair Z = {h, __fadd_rn(e, __fsub_rn(__fsub_rn(d.z0_l, pe), __fmul_rn(zf, d.dz_l)))};
+  return bp_mul({d.kv_h, d.kv_l}, Z);
+}
+
+// Per (column, view): r = 1 / Vx and the detector column coordinate
+// y = half_u / du - W / Vx of voxel column (sf, tf), both as pairs, and
+// q = W / Vx rounded (|q| > half_u / du is the reference's |u'| > half_u,
+// recon/bp3d20.cpp:116).
+__device__ __forceinline__ void bp_column_exact(const FdkDev& d, const BpView& v, float sf,
+                                                float tf, Fpair* r, Fpair* y, float* q) {
+  const float sx = fmaf(sf, v.bh, fmaf(tf, v.ch, v.ah));  // exact
+  const float lx = fmaf(sf, v.bl, fmaf(tf, v.cl, v.al));
+  const float sw = fmaf(sf, v.eh, fmaf(tf, v.fh, v.dh));  // exact
+  const float lw = fmaf(sf, v.el, fmaf(tf, v.fl, v.dl));
+  *r = bp_recip(sx, lx);
+  const Fpair qq = bp_mul({sw, lw}, *r);
+  *q = qq.h;
+  *y = bp_sub({d.yc_h, d.yc_l}, qq);
+}
+
+// floor(v) for |v| < 2^22, as a float and as an int, without conversions:
+// v + 1.5 * 2^23 rounded down lies in [2^23, 2^24), where floats are the
+// integers, and its bits minus those of 1.5 * 2^23 are floor(v).
+__device__ __forceinline__ float bp_floor(float v, int* vi) {
+  const float t = __fadd_rd(v, 12582912.0f);
+  *vi = (int)(__float_as_uint(t) - 0x4B400000u);
+  return __fsub_rn(t, 12582912.0f);
+}
+
 // The part of bp_coef that depends only on the voxel column (X, Y) and the
 // view: computed once per column by loops that walk a column along z.
 struct BpColumn {
-  float kk;        // sdd / Vx, the magnification
-  float up, y;     // detector u' and column coordinate
+  Fpair r;         // 1 / Vx
+  float q;         // W / Vx = half_u / du - y, rounded
+  float y;         // detector column coordinate, rounded
   float ts;        // the signed in-plane term of the distance weight
   float w;         // D^2 / (D - d)^2
-  float fy;        // column fraction
+  float fy;        // column fraction (to ~1e-8)
   int yi;          // column index
   bool near;       // u' or y near a discontinuity of the operator
   bool out;        // rejected whatever z (|u'| > half_u or y outside [0, ymax])
@@ -262,50 +376,50 @@ static __device__ __noinline__ bool bp_ts_negative(double x0d, double y0d, doubl
 
 __device__ __forceinline__ void bp_column(const FdkDev& d, const BpView& v, const BpViewD& vd,
                                           int s, int t, float X, float Y, BpColumn* c) {
-  float Vx, Vy;
-  bp_view_frame(d, v, X, Y, &Vx, &Vy);
-  c->kk = d.sdd / Vx;
-  c->up = Vy * c->kk;
-  c->y = bp_scale(d.half_u - c->up, d.inv_du, d.inv_du_lo);
+  Fpair y;
+  bp_column_exact(d, v, (float)s, (float)t, &c->r, &y, &c->q);
+  c->y = y.h;
   c->ts = X * v.c - Y * v.s;
-  c->near = fabsf(fabsf(c->up) - d.half_u) < 1e-4f * d.half_u ||
-            fabsf(c->y - d.ymax) < 1e-3f || fabsf(c->y) < 1e-3f;
-  c->out = fabsf(c->up) > d.half_u || !(c->y >= 0.f && c->y <= d.ymax);
+  c->near = fabsf(fabsf(c->q) - d.yc_h) < 1e-4f * d.yc_h || fabsf(c->y - d.ymax) < 1e-3f ||
+            fabsf(c->y) < 1e-3f;
+  c->out = fabsf(c->q) > d.yc_h || !(c->y >= 0.f && c->y <= d.ymax);
   float tt = X * v.s + Y * v.c;
   float dd = fabsf(c->ts - v.tanb * tt) * v.rs;
   if (fabsf(c->ts) < 1e-4f ? bp_ts_negative(d.x0d, d.y0d, d.dvoxd, &vd, s, t) : c->ts < 0.f)
     dd = -dd;
   float den = d.D - dd;
   c->w = (d.D * d.D) / (den * den);
-  c->yi = (int)c->y;
-  c->fy = c->y - (float)c->yi;
+  const float yf = bp_floor(y.h, &c->yi);
+  c->fy = __fadd_rn(__fsub_rn(y.h, yf), y.l);
 }
 
 // Coefficients of one voxel-view pair of the backprojection operator:
 // vol[s,t,z] += w * factor * bilinear(F_k; xi + fx, yi + fy).  Returns false
 // when the pair contributes nothing (rejected by recon/bp3d20.cpp:116, or
-// outside the interpolation guard of :152).  The plain backprojector and
-// its adjoint (the forward projector) both use it (directly or as
-// bp_column + bp_coef_z, the same operations), so the two are exact
-// transposes of each other.  Pairs within a small margin of a discontinuity
-// are decided in double (bp_ref_voxel).
+// outside the interpolation guard of :152).  m = bp_zterm(d, z).  The plain
+// backprojector and its adjoint (the forward projector) both use it
+// (directly or as bp_column + bp_coef_z, the same operations), so the two
+// are exact transposes of each other.  Pairs within a small margin of a
+// discontinuity are decided in double (bp_ref_voxel).
 __device__ __forceinline__ bool bp_coef_z(const FdkDev& d, const BpColumn& c, const BpViewD& vd,
-                                          int s, int t, int z, float Z, int* xi, int* yi,
-                                          float* fx, float* fy, float* w) {
-  float vp = Z * c.kk;
-  float x = bp_scale(d.half_v - vp, d.inv_dv, d.inv_dv_lo);
-  const bool near = c.near || fabsf(fabsf(vp) - d.half_v) < 1e-4f * d.half_v ||
-                    fabsf(x - d.xmax) < 1e-3f || fabsf(x) < 1e-3f;
+                                          int s, int t, int z, Fpair m, int* xi, int* yi,
+                                          float* fx, float* fy, float* w,
+                                          bool* in_double = nullptr) {
+  const Fpair p = bp_mul(m, c.r);  // Z sdd / (dv Vx) = half_v / dv - x
+  const Fpair x = bp_sub({d.xc_h, d.xc_l}, p);
+  const bool near = c.near || fabsf(fabsf(p.h) - d.xc_h) < 1e-4f * d.xc_h ||
+                    fabsf(x.h - d.xmax) < 1e-3f || fabsf(x.h) < 1e-3f;
   if (!near) {
-    if (c.out || fabsf(vp) > d.half_v || !(x >= 0.f && x <= d.xmax)) return false;
+    if (c.out || fabsf(p.h) > d.xc_h || !(x.h >= 0.f && x.h <= d.xmax)) return false;
     *w = c.w;
-    *xi = (int)x;
+    const float xf = bp_floor(x.h, xi);
+    *fx = __fadd_rn(__fsub_rn(x.h, xf), x.l);
     *yi = c.yi;
-    *fx = x - (float)*xi;
     *fy = c.fy;
     return true;
   }
   double xd, yd, wd;
+  if (in_double) *in_double = true;
   if (!bp_ref_voxel(d, vd, s, t, z, &xd, &yd, &wd)) return false;
   if (!(xd >= 0.0 && xd <= (double)d.nv && yd >= 0.0 && yd <= (double)d.nu)) return false;
   *w = (float)wd;
@@ -316,13 +430,14 @@ __device__ __forceinline__ bool bp_coef_z(const FdkDev& d, const BpColumn& c, co
   return true;
 }
 
-// bp_column + bp_coef_z for one voxel.
+// bp_column + bp_coef_z for one voxel (m = bp_zterm(d, z)).
 __device__ __forceinline__ bool bp_coef(const FdkDev& d, const BpView& v, const BpViewD& vd, int s,
-                                        int t, int z, float X, float Y, float Z, int* xi, int* yi,
-                                        float* fx, float* fy, float* w) {
+                                        int t, int z, float X, float Y, Fpair m, int* xi, int* yi,
+                                        float* fx, float* fy, float* w,
+                                        bool* in_double = nullptr) {
   BpColumn c;
   bp_column(d, v, vd, s, t, X, Y, &c);
-  return bp_coef_z(d, c, vd, s, t, z, Z, xi, yi, fx, fy, w);
+  return bp_coef_z(d, c, vd, s, t, z, m, xi, yi, fx, fy, w, in_double);
 }
 
 // Bilinear read at integer corner (xi, yi) with fractions (fx, fy), with the

@@ -33,11 +33,13 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
                                                         const float* __restrict__ vol_z,
                                                         const unsigned char* __restrict__ occ,
                                                         float* __restrict__ out) {
-  extern __shared__ float G[];  // [FP_COLS][nv]: column-major
+  extern __shared__ float G[];  // [FP_COLS][nv]: column-major, then nz z-terms
+  Fpair* zterm = reinterpret_cast<Fpair*>(G + FP_COLS * d.nv);
   const int k = blockIdx.y;
   const int c0 = blockIdx.x * FP_COLS;
   const int ncols = min(FP_COLS, d.nu - c0);
   for (int i = threadIdx.x; i < d.nv * FP_COLS; i += FP_THREADS) G[i] = 0.f;
+  for (int z = threadIdx.x; z < d.nz; z += FP_THREADS) zterm[z] = bp_zterm(d, z);
   __syncthreads();
   const BpView v = views[k];
   const BpViewD& vd = viewsd[k];
@@ -99,10 +101,9 @@ __global__ void __launch_bounds__(FP_THREADS) fp_kernel(FdkDev d, const BpView* 
         // coefficients (most voxels of a phantom in air are empty)
         const float r = __ldg(src + z);
         if (r == 0.f) continue;
-        const float Z = fmaf(-(float)z, d.dvox, d.z0);
         int xi, yi;
         float fx, fy, w;
-        if (!bp_coef_z(d, col, vd, s, t, z, Z, &xi, &yi, &fx, &fy, &w)) continue;
+        if (!bp_coef_z(d, col, vd, s, t, z, zterm[z], &xi, &yi, &fx, &fy, &w)) continue;
         const float c = w * r * v.factor;
 #pragma unroll
         for (int dy = 0; dy < 2; dy++) {
@@ -231,7 +232,7 @@ cudaError_t launch_fdk_forward_project(const FdkDev& d, const BpView* views, con
                                                                                  vol_z, occ);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  size_t smem = (size_t)d.nv * FP_COLS * sizeof(float);
+  size_t smem = (size_t)d.nv * FP_COLS * sizeof(float) + (size_t)d.nz * sizeof(Fpair);
   e = cudaFuncSetAttribute(fp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   dim3 grid((d.nu + FP_COLS - 1) / FP_COLS, d.n_views);

@@ -60,6 +60,16 @@ FdkDev make_fdk_dev(const monte_fdk_geom& g) {
   // 0 <= x <= nv and 0 <= y <= nu.
   d.xmax = (float)std::fmin((double)g.nv, 2.0 * g.half_v / g.dv);
   d.ymax = (float)std::fmin((double)g.nu, 2.0 * g.half_u / g.du);
+  auto split = [](double v, float* h, float* l) {
+    *h = (float)v;
+    *l = (float)(v - (double)*h);
+  };
+  split(g.half_u / g.du, &d.yc_h, &d.yc_l);
+  split(g.half_v / g.dv, &d.xc_h, &d.xc_l);
+  split(g.sdd / g.dv, &d.kv_h, &d.kv_l);
+  split(g.sdd * g.dvox / g.dv, &d.kb_h, &d.kb_l);
+  split(g.z0, &d.z0_h, &d.z0_l);
+  split(g.dvox, &d.dz_h, &d.dz_l);
   return d;
 }
 
@@ -93,6 +103,26 @@ int fdk_validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid) {
   return MONTE_OK;
 }
 
+namespace {
+// a + i b + j c for integer 0 <= i < ni, 0 <= j < nj, split as exact parts
+// (multiples of one power of two q, large enough that every partial sum
+// a_h + j c_h + i b_h is a float: |sum| < 2^24 q) plus float remainders.
+void split_affine(double a, double b, double c, int ni, int nj, float* ah, float* bh, float* ch,
+                  float* al, float* bl, float* cl) {
+  const double m = std::fabs(a) + (ni - 1) * std::fabs(b) + (nj - 1) * std::fabs(c);
+  // one bit of headroom for the rounding of the parts to multiples of q
+  const double q = std::ldexp(1.0, (m > 0 ? (int)std::ceil(std::log2(m)) : 0) + 1 - 24);
+  const double a_h = std::nearbyint(a / q) * q, b_h = std::nearbyint(b / q) * q,
+               c_h = std::nearbyint(c / q) * q;
+  *ah = (float)a_h;
+  *bh = (float)b_h;
+  *ch = (float)c_h;
+  *al = (float)(a - a_h);
+  *bl = (float)(b - b_h);
+  *cl = (float)(c - c_h);
+}
+}  // namespace
+
 void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t) {
   const int nv_ = g->n_views, nu = g->nu, nv = g->nv;
   std::vector<BpView>& views = t->views;
@@ -115,6 +145,15 @@ void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t) {
     v.rs = (float)(1.0 / sqrt(1 + tanb * tanb));
     v.factor = (float)(beta_span * 2 * M_PI / 360 * g->scale * g->scale2);
     v.pad = 0.f;
+    // Vx = X c + Y s - start_x and W = (sdd / du) (Y c - X s) at
+    // X = x0 + i dvox, Y = y0 - j dvox: the reference's (X - px) c +
+    // (Y - py) s and (Y - py) c - (X - px) s (recon/bp3d20.cpp:103-110)
+    // with px = start_x c, py = start_x s
+    const double K = g->sdd / g->du;
+    split_affine(g->x0 * c + g->y0 * s - (double)start_x, g->dvox * c, -g->dvox * s, g->nx,
+                 g->ny, &v.ah, &v.bh, &v.ch, &v.al, &v.bl, &v.cl);
+    split_affine(K * (g->y0 * c - g->x0 * s), -K * g->dvox * s, -K * g->dvox * c, g->nx, g->ny,
+                 &v.dh, &v.eh, &v.fh, &v.dl, &v.el, &v.fl);
     viewsd[k].c = c;
     viewsd[k].s = s;
     viewsd[k].px = start_x * c - 0.f * s;  // recon/bp3d20.cpp:87-88
@@ -652,6 +691,20 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
 }
 
 int monte_fdk_last_bp_variant(const monte_ctx* ctx) { return ctx ? ctx->last_bp_variant : -1; }
+
+int monte_fdk_exact_counts(monte_ctx* ctx, uint64_t* counts, int reset) {
+  if (!ctx) return MONTE_EINVAL;
+  if (!counts) return set_error(ctx, MONTE_EINVAL, "null counts");
+  MONTE_TRY(enter(ctx));
+  unsigned long long* dc = reinterpret_cast<unsigned long long*>(ctx->d_status + kBpExactSlot);
+  unsigned long long h[2];
+  MONTE_CUDA(ctx, cudaMemcpyAsync(h, dc, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  if (reset) MONTE_CUDA(ctx, cudaMemsetAsync(dc, 0, sizeof(h), ctx->stream));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  counts[0] = h[0];
+  counts[1] = h[1];
+  return MONTE_OK;
+}
 
 int monte_fdk_last_host_ranges(const monte_ctx* ctx) { return ctx ? ctx->last_host_ranges : 0; }
 

@@ -34,12 +34,12 @@ __global__ void __launch_bounds__(256) bp_plain_kernel(FdkDev d, const BpView* _
   if (inside) {
     const float X = fmaf((float)s, d.dvox, d.x0);
     const float Y = fmaf(-(float)t, d.dvox, d.y0);
-    const float Z = fmaf(-(float)z, d.dvox, d.z0);
+    const Fpair m = bp_zterm(d, z);
     for (int k = 0; k < d.n_views; k++) {
       const BpView v = views[k];
       int xi, yi;
       float fx, fy, w;
-      if (!bp_coef(d, v, viewsd[k], s, t, z, X, Y, Z, &xi, &yi, &fx, &fy, &w)) continue;
+      if (!bp_coef(d, v, viewsd[k], s, t, z, X, Y, m, &xi, &yi, &fx, &fy, &w)) continue;
       float val = bp_bilinear_at(d, filtered, k, xi, yi, fx, fy);
       acc = fmaf(w * val, v.factor, acc);
     }

@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <string>
+#include <utility>
 #include <vector>
 
 #include "mc.cuh"
@@ -25,6 +27,40 @@ int check_mem(monte_ctx* ctx, int mem) {
 }
 
 }  // namespace
+
+int mc_build_macro(monte_ctx* ctx, const monte_mc_phantom* ph, const monte_xcom* x,
+                   bool labels_on_device, const mc_params& P, mc_local_tables* L,
+                   std::vector<uint16_t>* cls, std::vector<uint8_t>* key) {
+  mc_setup_local(ph, x, L);
+  const size_t cells = (size_t)P.mgx * P.mgy * P.mgz;
+  std::vector<uint64_t> bits(cells * 4);
+  if (labels_on_device) {
+    MONTE_TRY(ensure_slot(ctx, kScratchAux3, cells * 4 * sizeof(uint64_t), "macro-cell label sets"));
+    unsigned long long* db = (unsigned long long*)ctx->scratch[kScratchAux3].ptr;
+    cudaError_t e = launch_mc_macro_bits(ph->labels, P, db, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "macro-cell label sets");
+    MONTE_CUDA(ctx, cudaMemcpyAsync(bits.data(), db, bits.size() * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } else {
+    mc_macro_bits_host(ph, ph->labels, &P, bits.data());
+  }
+  if (key) {
+    // the class grid depends on the grid, mu per label and the label sets
+    const int dims[4] = {P.mgx, P.mgy, P.mgz, P.mshift};
+    key->resize(sizeof(dims) + sizeof(L->mu) + bits.size() * sizeof(uint64_t));
+    uint8_t* k = key->data();
+    memcpy(k, dims, sizeof(dims));
+    memcpy(k + sizeof(dims), L->mu, sizeof(L->mu));
+    memcpy(k + sizeof(dims) + sizeof(L->mu), bits.data(), bits.size() * sizeof(uint64_t));
+    if (*key == ctx->mc_macro_key) return MONTE_OK;  // cls left empty: reuse the device copy
+  }
+  cls->assign(cells, 0);
+  if (mc_macro_classes(&P, L, bits.data(), cls->data()) != MONTE_OK)
+    return set_error(ctx, MONTE_ENOMEM, "out of host memory for the majorant classes");
+  return MONTE_OK;
+}
+
 }  // namespace monte
 
 using namespace monte;
@@ -141,6 +177,26 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
   mc_setup_views(g, V.data());
   mc_setup_pixels(g, U.data(), W.data());
   MONTE_TRY(enter(ctx));
+  const bool local = (P.flags & MC_F_LOCAL_MAJORANT) != 0;
+  if (local) {
+    // the tables and class grid of the last call are reused when they were
+    // built from the same phantom contents and tables
+    std::vector<uint16_t> cls;
+    std::vector<mc_local_tables> Lt(1);
+    std::vector<uint8_t> key;
+    MONTE_TRY(mc_build_macro(ctx, ph, xcom, mem == MONTE_MEM_DEVICE, P, Lt.data(), &cls, &key));
+    if (!cls.empty()) {
+      ctx->mc_macro_key.clear();
+      MONTE_TRY(ensure(ctx, ctx->mc_mclass, cls.size() * 2 + sizeof(mc_local_tables),
+                       "local majorant tables"));
+      MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->mc_mclass.ptr, Lt.data(), sizeof(mc_local_tables),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+      MONTE_CUDA(ctx, cudaMemcpyAsync((char*)ctx->mc_mclass.ptr + sizeof(mc_local_tables),
+                                      cls.data(), cls.size() * 2, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+      ctx->mc_macro_key.swap(key);
+    }
+  }
   MONTE_TRY(ensure(ctx, ctx->mc_tables, sizeof(mc_tables), "MC tables"));
   MONTE_TRY(ensure(ctx, ctx->mc_views, V.size() * sizeof(mc_view), "MC view table"));
   MONTE_TRY(ensure(ctx, ctx->mc_pixels, (U.size() + W.size()) * sizeof(mc_pixel), "MC pixel table"));
@@ -173,16 +229,20 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
     dscat = (int64_t*)ctx->scratch[kScratchMcScatter].ptr;
   }
   McDev d;
+  memset(&d, 0, sizeof(d));
   d.P = P;
   d.T = (const mc_tables*)ctx->mc_tables.ptr;
   d.V = (const mc_view*)ctx->mc_views.ptr;
   d.U = dpix;
   d.W = dpix + U.size();
   d.labels = dlab;
+  d.L = local ? (const mc_local_tables*)ctx->mc_mclass.ptr : nullptr;
+  d.mclass = local ? (const uint16_t*)((const char*)ctx->mc_mclass.ptr + sizeof(mc_local_tables))
+                   : nullptr;
   d.prim = (unsigned long long*)dprim;
   d.scat = (unsigned long long*)dscat;
   d.stats = dstat;
-  d.counter = dstat + 8;
+  d.counter = dstat + 12;
   d.total = total;
   if (total) {
     cudaError_t e = launch_mc(d, run->kernel, ctx->sm_count, ctx->stream);
@@ -193,18 +253,107 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
     MONTE_CUDA(ctx, cudaMemcpyAsync(scatter, dscat, ncell * 8, cudaMemcpyDeviceToHost, ctx->stream));
   }
   if (stats || mem == MONTE_MEM_HOST) {
-    unsigned long long h[8];
+    unsigned long long h[kMcStats];
     MONTE_CUDA(ctx, cudaMemcpyAsync(h, dstat, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (stats) {
-      stats->histories = h[0];
-      stats->woodcock_steps = h[1];
-      stats->interactions = h[2];
-      stats->primary_counts = h[3];
-      stats->scatter_counts = h[4];
-      stats->dropped = h[5];
-    }
+    if (stats) mc_stats_from(h, stats);
   }
+  return MONTE_OK;
+}
+
+int monte_spectrum_from_cumulative(const float* cum, int32_t n_bins, double bin_kev,
+                                   double fallback_kev, double* energy_kev, double* weight,
+                                   int32_t* n_lines) {
+  if (!cum || !energy_kev || !weight || !n_lines || n_bins <= 0 || n_bins + 1 > MC_MAX_LINES ||
+      !(bin_kev > 0) || !(fallback_kev > 0))
+    return MONTE_EINVAL;
+  // u is uniform on (0, 1]; bin d takes the part of [cum[d], cum[d+1]]
+  // inside (0, 1] that no earlier bin took (the reference's loop breaks at
+  // the first match).  `taken` is the union of the earlier intervals as
+  // disjoint sorted pieces.
+  std::vector<std::pair<double, double>> taken;
+  double total = 0.0;
+  for (int d = 0; d < n_bins; d++) {
+    double a = std::fmax((double)cum[d], 0.0), b = std::fmin((double)cum[d + 1], 1.0);
+    double w = 0.0;
+    if (b > a) {
+      w = b - a;
+      for (const auto& t : taken) w -= std::fmax(0.0, std::fmin(b, t.second) - std::fmax(a, t.first));
+      std::vector<std::pair<double, double>> merged;
+      bool placed = false;
+      for (const auto& t : taken) {
+        if (t.second < a || t.first > b) {
+          if (!placed && t.first > b) {
+            merged.push_back({a, b});
+            placed = true;
+          }
+          merged.push_back(t);
+        } else {
+          a = std::fmin(a, t.first);
+          b = std::fmax(b, t.second);
+        }
+      }
+      if (!placed) merged.push_back({a, b});
+      taken.swap(merged);
+    }
+    energy_kev[d] = (d + 1) * bin_kev;
+    weight[d] = std::fmax(w, 0.0);
+    total += weight[d];
+  }
+  energy_kev[n_bins] = fallback_kev;
+  weight[n_bins] = std::fmax(1.0 - total, 0.0);
+  *n_lines = n_bins + 1;
+  return MONTE_OK;
+}
+
+int monte_parse_numbers(const char* text, size_t len, float* values, int32_t max_values,
+                        int32_t* n_values) {
+  if (!text || !values || !n_values || max_values < 0) return MONTE_EINVAL;
+  std::string buf(text, len);
+  const char* p = buf.c_str();
+  int n = 0;
+  while (n < max_values) {
+    char* end = nullptr;
+    const float v = strtof(p, &end);
+    if (end == p) break;
+    values[n++] = v;
+    p = end;
+  }
+  *n_values = n;
+  return MONTE_OK;
+}
+
+int monte_mc_sample_energies(monte_ctx* ctx, const monte_spectrum* spec, uint64_t seed,
+                             uint32_t job, uint64_t n, float* energies, int mem) {
+  if (!ctx) return MONTE_EINVAL;
+  if (!spec || (!energies && n)) return set_error(ctx, MONTE_EINVAL, "null argument");
+  MONTE_TRY(check_mem(ctx, mem));
+  std::vector<mc_tables> T(1);
+  memset(T.data(), 0, sizeof(mc_tables));
+  const char* why = "";
+  if (mc_setup_spectrum(spec, T.data(), &why) != MONTE_OK)
+    return set_error(ctx, MONTE_EINVAL, "%s", why);
+  if (n == 0) return MONTE_OK;
+  if (n > ((uint64_t)1 << 40)) return set_error(ctx, MONTE_EOVERFLOW, "too many samples");
+  MONTE_TRY(enter(ctx));
+  MONTE_TRY(ensure(ctx, ctx->mc_tables, sizeof(mc_tables), "MC tables"));
+  MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->mc_tables.ptr, T.data(), sizeof(mc_tables),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  float* dout = energies;
+  if (mem == MONTE_MEM_HOST) {
+    MONTE_TRY(ensure_slot(ctx, kScratchAux0, n * sizeof(float), "energy staging"));
+    dout = (float*)ctx->scratch[kScratchAux0].ptr;
+  }
+  monte_philox_keys keys;
+  monte_philox_schedule(seed, &keys);
+  cudaError_t e = launch_mc_energies((const mc_tables*)ctx->mc_tables.ptr, seed, keys, job, n,
+                                     dout, ctx->sm_count, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "energy sampling launch");
+  if (mem == MONTE_MEM_HOST)
+    MONTE_CUDA(ctx, cudaMemcpyAsync(energies, dout, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+  // the host table dies at return
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return MONTE_OK;
 }
 

@@ -62,9 +62,9 @@ __device__ __forceinline__ void decompose(const McDev& d, unsigned long long h, 
   *iv = d.P.v_begin + (int)(pix % nv_roi);
 }
 
-__device__ __forceinline__ void warp_stats(const McDev& d, unsigned long long v[6]) {
+__device__ __forceinline__ void warp_stats(const McDev& d, unsigned long long v[kMcStats]) {
 #pragma unroll
-  for (int i = 0; i < 6; i++) {
+  for (int i = 0; i < kMcStats; i++) {
     unsigned long long x = v[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -72,11 +72,22 @@ __device__ __forceinline__ void warp_stats(const McDev& d, unsigned long long v[
   }
 }
 
+// The kind of the interaction a collision led to (none when the history
+// had used its interactions), into st[6..8]; constant indices keep st in
+// registers.
+__device__ __forceinline__ void count_event(const mc_photon& p, int n_before,
+                                            unsigned long long (&st)[kMcStats]) {
+  if (p.n_int == n_before) return;
+  if (p.last == MC_EV_RAYLEIGH) st[6]++;
+  else if (p.last == MC_EV_COMPTON) st[7]++;
+  else st[8]++;
+}
+
 __global__ void __launch_bounds__(128) mc_plain_kernel(McDev d) {
   const int nv_roi = d.P.v_end - d.P.v_begin;
   const int nu_roi = d.P.u_end - d.P.u_begin;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long st[kMcStats] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (idx < nu_roi * nv_roi) {
     const int iu = d.P.u_begin + idx / nv_roi;
     const int iv = d.P.v_begin + idx % nv_roi;
@@ -87,11 +98,12 @@ __global__ void __launch_bounds__(128) mc_plain_kernel(McDev d) {
         st[0]++;
         while (true) {
           if (p.state == MC_FLY) {
-            mc_flight_step(&d.P, d.T, d.labels, &p);
-            st[1]++;
+            if (mc_flight_event(&d.P, d.T, d.L, d.labels, d.mclass, &p)) st[1]++; else st[9]++;
             if (p.state == MC_DEAD) st[5]++;
           } else if (p.state == MC_COLLIDED) {
+            const int n0 = p.n_int;
             p.state = mc_after_collision(&d.P, d.T, &p);
+            count_event(p, n0, st);
           } else if (p.state == MC_ESCAPED) {
             int kind = mc_tally_kind(&d.P, &p);
             long long cell = mc_detector_index(&d.P, d.V, &p);
@@ -118,7 +130,7 @@ __device__ __forceinline__ void persistent_body(const McDev& d) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
-  unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long st[kMcStats] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   mc_photon p;
   p.state = MC_DEAD;
   p.n_int = 0;
@@ -162,8 +174,7 @@ __device__ __forceinline__ void persistent_body(const McDev& d) {
     // ---- a few Woodcock steps ------------------------------------------
 #pragma unroll 1
     for (int i = 0; i < SR && p.state == MC_FLY; i++) {
-      mc_flight_step(&d.P, d.T, d.labels, &p);
-      st[1]++;
+      if (mc_flight_event(&d.P, d.T, d.L, d.labels, d.mclass, &p)) st[1]++; else st[9]++;
       if (p.state == MC_DEAD) st[5]++;
     }
     // ---- escaped photons: warp-aggregated tally --------------------------
@@ -188,7 +199,11 @@ __device__ __forceinline__ void persistent_body(const McDev& d) {
     const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
     const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
     if (coll && (__popc(coll) >= CB || fly == 0)) {
-      if (p.state == MC_COLLIDED) p.state = mc_after_collision(&d.P, d.T, &p);
+      if (p.state == MC_COLLIDED) {
+        const int n0 = p.n_int;
+        p.state = mc_after_collision(&d.P, d.T, &p);
+        count_event(p, n0, st);
+      }
     }
   }
   st[2] += (unsigned long long)p.n_int;
@@ -217,7 +232,7 @@ __global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
   __shared__ unsigned long long s_starts[kMaxBatchJobs + 1];
   for (int i = threadIdx.x; i <= n_jobs; i += blockDim.x) s_starts[i] = starts[i];
   __syncthreads();
-  unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long st[kMcStats] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   mc_photon p;
   p.state = MC_DEAD;
   p.n_int = 0;
@@ -266,8 +281,7 @@ __global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
     if (__all_sync(FULL, retired)) break;
 #pragma unroll 1
     for (int i = 0; i < kStepsPerRound && p.state == MC_FLY; i++) {
-      mc_flight_step(&J->P, J->T, J->labels, &p);
-      st[1]++;
+      if (mc_flight_event(&J->P, J->T, J->L, J->labels, J->mclass, &p)) st[1]++; else st[9]++;
       if (p.state == MC_DEAD) st[5]++;
     }
     long long cell = -1;
@@ -290,16 +304,55 @@ __global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
     const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
     const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
     if (coll && (__popc(coll) >= kCollideBatch || fly == 0)) {
-      if (p.state == MC_COLLIDED) p.state = mc_after_collision(&J->P, J->T, &p);
+      if (p.state == MC_COLLIDED) {
+        const int n0 = p.n_int;
+        p.state = mc_after_collision(&J->P, J->T, &p);
+        count_event(p, n0, st);
+      }
     }
   }
   st[2] += (unsigned long long)p.n_int;
 #pragma unroll
-  for (int i = 0; i < 6; i++) {
+  for (int i = 0; i < kMcStats; i++) {
     unsigned long long x = st[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
     if (lane == 0 && x) atomicAdd(&stats[i], x);
+  }
+}
+
+// One CTA per macro cell: the cell's voxels OR their label bits into a
+// shared 256-bit set, written once.
+__global__ void __launch_bounds__(128) mc_macro_bits_kernel(const uint8_t* __restrict__ labels,
+                                                            int nx, int ny, int nz, int shift,
+                                                            int gx, int gy,
+                                                            unsigned long long* __restrict__ bits) {
+  __shared__ unsigned long long set[4];
+  if (threadIdx.x < 4) set[threadIdx.x] = 0;
+  __syncthreads();
+  const int c = blockIdx.x;
+  const int cx = c % gx, cy = (c / gx) % gy, cz = c / (gx * gy);
+  const int m = 1 << shift;
+  const int x0 = cx << shift, y0 = cy << shift, z0 = cz << shift;
+  for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
+    const int x = x0 + (i & (m - 1)), y = y0 + ((i >> shift) & (m - 1)), z = z0 + (i >> (2 * shift));
+    if (x < nx && y < ny && z < nz) {
+      const int l = labels[((size_t)z * ny + y) * nx + x];
+      atomicOr(&set[l >> 6], 1ull << (l & 63));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) bits[(size_t)c * 4 + threadIdx.x] = set[threadIdx.x];
+}
+
+__global__ void mc_energy_kernel(const mc_tables* __restrict__ T, uint64_t seed,
+                                 monte_philox_keys keys, uint32_t job, unsigned long long n,
+                                 float* __restrict__ out) {
+  for (unsigned long long h = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; h < n;
+       h += (unsigned long long)gridDim.x * blockDim.x) {
+    monte_stream rng;
+    monte_stream_init(&rng, seed, h, job);
+    out[h] = T->n_lines > 1 ? mc_sample_energy(T, monte_uniform_keys(&rng, &keys)) : T->energy[0];
   }
 }
 
@@ -352,6 +405,25 @@ cudaError_t launch_mc_batch(const McDev* jobs, const unsigned long long* starts,
   if (per_sm < 1) per_sm = 1;
   mc_persistent_batch_kernel<<<sm_count * per_sm, 256, 0, st>>>(jobs, starts, n_jobs, total,
                                                                 counter, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mc_macro_bits(const uint8_t* labels, const mc_params& P, unsigned long long* bits,
+                                 cudaStream_t st) {
+  const unsigned cells = (unsigned)P.mgx * P.mgy * P.mgz;
+  if (cells == 0) return cudaSuccess;
+  mc_macro_bits_kernel<<<cells, 128, 0, st>>>(labels, P.nx, P.ny, P.nz, P.mshift, P.mgx, P.mgy,
+                                              bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mc_energies(const mc_tables* T, uint64_t seed, const monte_philox_keys& keys,
+                               uint32_t job, unsigned long long n, float* out, int sm_count,
+                               cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const unsigned long long want = (n + 255) / 256;
+  const unsigned blocks = (unsigned)(want < 8ull * sm_count ? want : 8ull * sm_count);
+  mc_energy_kernel<<<blocks, 256, 0, st>>>(T, seed, keys, job, n, out);
   return cudaGetLastError();
 }
 

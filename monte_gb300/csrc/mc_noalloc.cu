@@ -21,8 +21,16 @@
 //    MONTE_NOALLOC_MAX_PIXELS detector pixels along each axis; larger
 //    requests are rejected with MONTE_EINVAL.
 //  * The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    (cudaGetSymbolAddress) with that device current and keeps it for the
+//    life of the process; a cudaDeviceReset on that device between calls
+//    would leave it stale, so do not reset a device this entry point has
+//    used.
+//  * The call cannot be captured into a CUDA graph: its tables go up from
+//    host staging that the next call overwrites, and with statistics it
+//    waits for the stream.  A call on a capturing stream returns
+//    MONTE_EUNSUPPORTED before it issues any work.
+//  * labels, primary and scatter must be device memory (or managed);
+//    anything else is rejected with MONTE_EINVAL.
 //  * Every call on a device shares the array and leaves the last call's
 //    tables in it.  Each call re-initialises what it needs (tables, counter
 //    and statistics are written before its kernel starts), but two calls
@@ -44,7 +52,7 @@ struct NoallocScratch {
   mc_tables tables;
   mc_view views[MONTE_NOALLOC_MAX_VIEWS];
   mc_pixel pixels[2 * MONTE_NOALLOC_MAX_PIXELS];
-  unsigned long long stats[8];
+  unsigned long long stats[12];
   unsigned long long counter[8];
 };
 
@@ -78,6 +86,16 @@ int scratch_address(int dev, NoallocScratch** out) {
   return MONTE_OK;
 }
 
+// Whether p is memory the GPU can address directly (device or managed).
+bool device_addressable(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
 // Host staging for the tables: per thread, static storage (no allocation).
 thread_local mc_tables tl_tables;
 thread_local mc_view tl_views[MONTE_NOALLOC_MAX_VIEWS];
@@ -100,6 +118,26 @@ extern "C" int monte_mc_run_noalloc(const monte_mc_geom* g, const monte_mc_phant
                      "monte_mc_run_noalloc: %d views of %d x %d pixels exceed its static scratch "
                      "(at most %d views and %d pixels per axis)",
                      g->n_views, g->nu, g->nv, MONTE_NOALLOC_MAX_VIEWS, MONTE_NOALLOC_MAX_PIXELS);
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)cuda_stream, &cs);
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(nullptr, ce, "monte_mc_run_noalloc: stream query");
+    }
+    if (cs != cudaStreamCaptureStatusNone)
+      return set_error(nullptr, MONTE_EUNSUPPORTED,
+                       "monte_mc_run_noalloc: the stream is being captured; this call cannot "
+                       "be part of a CUDA graph");
+  }
+  if (!device_addressable(ph->labels) || !device_addressable(primary) ||
+      !device_addressable(scatter))
+    return set_error(nullptr, MONTE_EINVAL,
+                     "monte_mc_run_noalloc: labels, primary and scatter must be device memory");
+  if (g->flags & MONTE_MC_LOCAL_MAJORANT)
+    return set_error(nullptr, MONTE_EUNSUPPORTED,
+                     "monte_mc_run_noalloc: MONTE_MC_LOCAL_MAJORANT needs per-phantom tables "
+                     "that its static scratch does not hold");
   mc_params P;
   const char* why = "";
   if (mc_setup_params(g, ph, run, &P, &why) != MONTE_OK)
@@ -135,6 +173,7 @@ extern "C" int monte_mc_run_noalloc(const monte_mc_geom* g, const monte_mc_phant
   if (e == cudaSuccess) e = cudaMemsetAsync(S->stats, 0, sizeof(S->stats) + sizeof(S->counter), st);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "monte_mc_run_noalloc: table upload");
   McDev d;
+  memset(&d, 0, sizeof(d));
   d.P = P;
   d.T = &S->tables;
   d.V = S->views;
@@ -151,16 +190,11 @@ extern "C" int monte_mc_run_noalloc(const monte_mc_geom* g, const monte_mc_phant
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "monte_mc_run_noalloc: launch");
   }
   if (stats) {
-    unsigned long long h[8];
+    unsigned long long h[kMcStats];
     e = cudaMemcpyAsync(h, S->stats, sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "monte_mc_run_noalloc: statistics");
-    stats->histories = h[0];
-    stats->woodcock_steps = h[1];
-    stats->interactions = h[2];
-    stats->primary_counts = h[3];
-    stats->scatter_counts = h[4];
-    stats->dropped = h[5];
+    mc_stats_from(h, stats);
   }
   return MONTE_OK;
 }

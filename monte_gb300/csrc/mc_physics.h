@@ -28,11 +28,18 @@ extern "C" {
 #define MC_MAX_LINES 512
 #define MC_MAX_STEPS (1 << 22)   /* Woodcock steps per flight before a history is dropped */
 #define MC_MAX_KN_TRIES 4096     /* Kahn rejection attempts before a history is dropped */
+#define MC_MAX_CLASSES 64        /* majorant classes of the macro-cell grid */
 
 /* physics switches (public values in include/monte.h) */
 #define MC_F_STALE_SIN_PHI 0x1u    /* 2nd+ Compton keeps the emission sin_phi_a (CBCT_real325im.cu:768-773) */
 #define MC_F_FIRST_COMPTON_Z 0x2u  /* 1st Compton turns about +z (CBCT_real2.cpp:193,460-463) */
 #define MC_F_NO_RAYLEIGH_TALLY 0x4u /* flights after a Rayleigh event are not tallied (CBCT_real2.cpp:373-397) */
+#define MC_F_LOCAL_MAJORANT 0x8u   /* majorants per macro cell (mc_flight_leg) */
+
+/* Majorant of a macro-cell class at one energy bin, and its reciprocal. */
+typedef struct {
+  float maj, inv;
+} mc_majorant;
 
 /* Tables of one run, built on the host. */
 typedef struct {
@@ -45,12 +52,23 @@ typedef struct {
   float p_photo[8][MC_NBINS];
   float p_photo_coh[8][MC_NBINS];
   int8_t label_material[MC_MAX_LABELS];  /* -1: air */
-  /* spectrum: inverse CDF over lines */
-  float cdf[MC_MAX_LINES];
+  /* spectrum: Walker's alias table over the lines (slot i keeps line i
+   * with probability alias_p[i], else gives line alias_i[i]) */
+  float alias_p[MC_MAX_LINES];
+  int16_t alias_i[MC_MAX_LINES];
   float energy[MC_MAX_LINES];
   int n_lines;
   int pad_;
 } mc_tables;
+
+/* Tables of the local majorants (MC_F_LOCAL_MAJORANT), built on the host:
+ * attenuation per label and bin (1/cm, table * density), and per
+ * macro-cell class the largest mu over the labels of the cells it stands
+ * for ({0, 3e38} for air only). */
+typedef struct {
+  float mu[MC_MAX_LABELS][MC_NBINS];
+  mc_majorant maj[MC_MAX_CLASSES][MC_NBINS];
+} mc_local_tables;
 
 /* Geometry and run parameters (float as the kernels use them). */
 typedef struct {
@@ -66,6 +84,12 @@ typedef struct {
   monte_philox_keys keys;    /* round keys of seed (monte_philox_schedule) */
   uint32_t job;
   uint64_t per;              /* histories per pixel per view */
+  /* macro-cell grid of the local majorants: cells of 2^mshift voxels per
+   * axis, mgx x mgy x mgz of them; `leg` (cm) = 2^mshift times the
+   * smallest voxel edge, the longest move from a point of a cell that
+   * stays within the cell and its neighbours */
+  int mgx, mgy, mgz, mshift;
+  float leg;
   int view_begin, view_end, u_begin, u_end, v_begin, v_end;
 } mc_params;
 
@@ -80,6 +104,7 @@ typedef struct {
 } mc_pixel;
 
 enum { MC_FLY = 0, MC_COLLIDED = 1, MC_ESCAPED = 2, MC_DEAD = 3 };
+enum { MC_EV_NONE = 0, MC_EV_RAYLEIGH = 1, MC_EV_COMPTON = 2, MC_EV_PHOTO = 3 };
 
 typedef struct {
   float x, y, z;
@@ -89,11 +114,14 @@ typedef struct {
   int kb;                /* energy bin (int)(E+0.5) */
   int label;             /* label at the last real collision */
   int n_int;             /* interactions done */
-  int last;              /* 0: none, 1: Rayleigh, 2: Compton (kind of the last interaction) */
+  int last;              /* kind of the last interaction: 0 none, 1 Rayleigh, 2 Compton,
+                            3 photoelectric (MC_EV_*) */
   int n_compton;         /* Compton events so far */
   int view, iu, iv;
   int state;
-  uint32_t steps;        /* Woodcock steps in the current flight */
+  uint32_t steps;        /* Woodcock steps (and majorant legs) in the current flight */
+  float tau;             /* optical depth left of the current exponential draw (local
+                            majorants; 0: draw a new one) */
   monte_stream rng;
 } mc_photon;
 
@@ -146,6 +174,19 @@ MONTE_HD int mc_box_span(const mc_params* P, float ox, float oy, float oz, float
   return lo < hi;
 }
 
+/* Source energy from a uniform u in (0, 1] by the alias table: slot
+ * i = floor(n u), kept with probability alias_p[i] (the fraction n u - i
+ * decides), else its alias -- the same distribution as the reference's
+ * inverse-CDF search (CBCT_real325.cu:479-486) in constant time, with no
+ * data-dependent loop. */
+MONTE_HD float mc_sample_energy(const mc_tables* T, float u) {
+  const float x = u * (float)T->n_lines;
+  int i = (int)x;
+  if (i >= T->n_lines) i = T->n_lines - 1;
+  const float f = x - (float)i;
+  return T->energy[f < T->alias_p[i] ? i : (int)T->alias_i[i]];
+}
+
 /* Start a history: energy, emission direction aimed at pixel (iu, iv) of
  * view `view`, position on the start plane, then straight to the phantom
  * box (air streaming is exact: nothing interacts in air).
@@ -161,20 +202,12 @@ MONTE_HD void mc_start(const mc_params* P, const mc_tables* T, const mc_view* V,
   p->last = 0;
   p->n_compton = 0;
   p->steps = 0;
+  p->tau = 0.0f;
   p->label = 0;
-  /* spectrum (CBCT_real325im.cu:491-498): inverse CDF */
-  float E = T->energy[0];
-  if (T->n_lines > 1) {
-    float u = monte_uniform_keys(&p->rng, &P->keys);
-    int lo = 0, hi = T->n_lines - 1;
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      if (u <= T->cdf[mid]) hi = mid; else lo = mid + 1;
-    }
-    E = T->energy[lo];
-  }
-  p->E = E;
-  p->kb = mc_bin(E);
+  /* spectrum (CBCT_real325im.cu:491-498): one uniform per history */
+  p->E = T->n_lines > 1 ? mc_sample_energy(T, monte_uniform_keys(&p->rng, &P->keys))
+                        : T->energy[0];
+  p->kb = mc_bin(p->E);
   const mc_view* v = &V[view];
   const mc_pixel* pu = &U[iu];
   const mc_pixel* pv = &W[iv];
@@ -249,6 +282,83 @@ MONTE_HD void mc_flight_step(const mc_params* P, const mc_tables* T, const uint8
   }
 }
 
+/* One event of a flight with majorants local to macro cells
+ * (MC_F_LOCAL_MAJORANT; the reference's single majorant is mc_flight_step):
+ * delta tracking with a piecewise-constant majorant.  The photon carries
+ * tau, the optical depth left of its current exponential draw.  In the
+ * macro cell holding it, the majorant m of the cell's class bounds mu over
+ * the cell and its 26 neighbours, so over the next `leg` cm at least.  If
+ * tau / m fits in a leg the photon moves there and makes a tentative
+ * collision, accepted with probability mu(label) / m (a Woodcock step);
+ * otherwise it moves one leg and spends m * leg of tau (nothing can
+ * collide there beyond what m accounts for; exponential flights are
+ * memoryless).  Air-only cells (m = 0) are crossed a leg at a time.
+ * Returns 1 after a tentative collision, 0 after a leg; updates p->state. */
+MONTE_HD int mc_flight_leg(const mc_params* P, const mc_local_tables* L, const uint8_t* labels,
+                           const uint16_t* mclass, mc_photon* p) {
+  /* A photon that enters the box sits on a face (mc_start), and rounding
+   * can put it a hair outside: positions within half a voxel of the box
+   * count as inside, with the cell index clamped to the grid (nothing
+   * outside the box interacts; a tentative collision there escapes
+   * through mc_label_at).  Farther out the photon has left: the box is
+   * convex. */
+  const float fx = (p->x - P->x0) * P->inv_dx;
+  const float fy = (p->y - P->y0) * P->inv_dy;
+  const float fz = (p->z - P->z0) * P->inv_dz;
+  if (!(fx > -0.5f && fx < (float)P->nx + 0.5f && fy > -0.5f && fy < (float)P->ny + 0.5f &&
+        fz > -0.5f && fz < (float)P->nz + 0.5f)) {
+    p->state = MC_ESCAPED;
+    return 0;
+  }
+  int cx = (int)(fx > 0.0f ? fx : 0.0f) >> P->mshift;
+  int cy = (int)(fy > 0.0f ? fy : 0.0f) >> P->mshift;
+  int cz = (int)(fz > 0.0f ? fz : 0.0f) >> P->mshift;
+  cx = cx < P->mgx ? cx : P->mgx - 1;
+  cy = cy < P->mgy ? cy : P->mgy - 1;
+  cz = cz < P->mgz ? cz : P->mgz - 1;
+  const unsigned cr =
+      mclass[((size_t)cz * (size_t)P->mgy + (size_t)cy) * (size_t)P->mgx + (size_t)cx];
+  const mc_majorant m = L->maj[cr & 0xffu][p->kb];
+  const float leg = (float)(cr >> 8) * P->leg;  /* R legs: the class bounds mu that far */
+  if (p->tau <= 0.0f) p->tau = -monte_logf(monte_uniform_keys(&p->rng, &P->keys));
+  float dx, dy, dz;
+  mc_dir(p, &dx, &dy, &dz);
+  const float s = p->tau * m.inv;
+  p->steps++;
+  if (!(s <= leg)) {
+    p->x = fmaf(leg, dx, p->x);
+    p->y = fmaf(leg, dy, p->y);
+    p->z = fmaf(leg, dz, p->z);
+    p->tau = fmaf(-m.maj, leg, p->tau);
+    if (p->steps >= MC_MAX_STEPS) p->state = MC_DEAD;
+    return 0;
+  }
+  p->x = fmaf(s, dx, p->x);
+  p->y = fmaf(s, dy, p->y);
+  p->z = fmaf(s, dz, p->z);
+  p->tau = 0.0f;
+  const float nu = monte_uniform_keys(&p->rng, &P->keys);
+  const int lab = mc_label_at(P, labels, p->x, p->y, p->z);
+  if (lab < 0) {
+    p->state = MC_ESCAPED;
+  } else if (nu * m.maj <= L->mu[lab][p->kb]) {
+    p->label = lab;
+    p->state = MC_COLLIDED;
+  } else if (p->steps >= MC_MAX_STEPS) {
+    p->state = MC_DEAD;
+  }
+  return 1;
+}
+
+/* One event of a flight, by the run's transport: returns 1 for a
+ * Woodcock step, 0 for a majorant leg (local majorants only). */
+MONTE_HD int mc_flight_event(const mc_params* P, const mc_tables* T, const mc_local_tables* L,
+                             const uint8_t* labels, const uint16_t* mclass, mc_photon* p) {
+  if (P->flags & MC_F_LOCAL_MAJORANT) return mc_flight_leg(P, L, labels, mclass, p);
+  mc_flight_step(P, T, labels, p);
+  return 1;
+}
+
 /* Detector pixel hit by an escaped photon, as a flat index into the
  * [view][u][v] tally, or -1.  The line through the last position along the
  * current direction, in the view frame, meets the detector plane x' = dod
@@ -284,12 +394,16 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
   if (mat < 0) return MC_DEAD;
   float sc = monte_uniform_keys(&p->rng, &P->keys);
   p->n_int++;
-  if (sc <= T->p_photo[mat][p->kb]) return MC_DEAD;
+  if (sc <= T->p_photo[mat][p->kb]) {
+    p->last = MC_EV_PHOTO;
+    return MC_DEAD;
+  }
   if (sc <= T->p_photo_coh[mat][p->kb]) {
-    p->last = 1;
+    p->last = MC_EV_RAYLEIGH;
     p->steps = 0;
     return MC_FLY;
   }
+  p->last = MC_EV_COMPTON;
   /* Kahn's rejection sampling of lambda' = rho * lambda (:701-736) */
   float lambda = 511.0f / p->E;
   float lam2 = lambda + 2.0f;
@@ -349,7 +463,6 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
   p->cp = cpn;
   p->sp = spn;
   p->n_compton++;
-  p->last = 2;
   p->steps = 0;
   return MC_FLY;
 }
@@ -358,7 +471,7 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
  * 0 primary, 1 scatter, -1 not tallied. */
 MONTE_HD int mc_tally_kind(const mc_params* P, const mc_photon* p) {
   if (p->n_int == 0) return 0;
-  if (p->last == 1 && (P->flags & MC_F_NO_RAYLEIGH_TALLY)) return -1;
+  if (p->last == MC_EV_RAYLEIGH && (P->flags & MC_F_NO_RAYLEIGH_TALLY)) return -1;
   return 1;
 }
 

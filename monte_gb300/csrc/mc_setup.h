@@ -14,10 +14,29 @@
 #define MONTE_MC_SETUP_H
 
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "../../include/monte.h"
 #include "mc_physics.h"
+
+/* Macro-cell grid of the local majorants: cells of 2^mshift voxels per
+ * axis, the smallest power of two >= 2 that leaves at most 48 cells along
+ * the longest axis (a leg then spans ~2% of the phantom).  `leg` is
+ * 2^mshift times the smallest voxel edge, rounded down. */
+static inline void mc_macro_dims(const monte_mc_phantom* ph, mc_params* P) {
+  int n = ph->nx > ph->ny ? ph->nx : ph->ny;
+  if (ph->nz > n) n = ph->nz;
+  int sh = 1;
+  while (sh < 20 && ((n + (1 << sh) - 1) >> sh) > 48) sh++;
+  P->mshift = sh;
+  P->mgx = (ph->nx + (1 << sh) - 1) >> sh;
+  P->mgy = (ph->ny + (1 << sh) - 1) >> sh;
+  P->mgz = (ph->nz + (1 << sh) - 1) >> sh;
+  double d = ph->dx < ph->dy ? ph->dx : ph->dy;
+  if (ph->dz < d) d = ph->dz;
+  P->leg = (float)(ldexp(d, sh) * (1.0 - 1e-6));
+}
 
 /* Returns MONTE_OK or MONTE_EINVAL; `why` receives a message. */
 static inline int mc_setup_params(const monte_mc_geom* g, const monte_mc_phantom* ph,
@@ -29,7 +48,8 @@ static inline int mc_setup_params(const monte_mc_geom* g, const monte_mc_phantom
     return MONTE_EINVAL;
   }
   if (g->max_interactions < 0 || g->max_interactions > 1000) { *why = "bad max_interactions"; return MONTE_EINVAL; }
-  if (g->flags & ~(unsigned)(MONTE_MC_STALE_SIN_PHI | MONTE_MC_FIRST_COMPTON_Z | MONTE_MC_NO_RAYLEIGH_TALLY)) {
+  if (g->flags & ~(unsigned)(MONTE_MC_STALE_SIN_PHI | MONTE_MC_FIRST_COMPTON_Z |
+                             MONTE_MC_NO_RAYLEIGH_TALLY | MONTE_MC_LOCAL_MAJORANT)) {
     *why = "unknown MC flags";
     return MONTE_EINVAL;
   }
@@ -82,6 +102,61 @@ static inline int mc_setup_params(const monte_mc_geom* g, const monte_mc_phantom
   P->u_end = run->u_end;
   P->v_begin = run->v_begin;
   P->v_end = run->v_end;
+  mc_macro_dims(ph, P);
+  return MONTE_OK;
+}
+
+/* Spectrum lines -> energies and Walker's alias table (Vose's
+ * construction in double): n slots of probability 1/n each; slot i keeps
+ * line i with probability alias_p[i] and gives line alias_i[i] otherwise.
+ * Lines of zero weight are never drawn. */
+static inline int mc_setup_spectrum(const monte_spectrum* sp, mc_tables* T, const char** why) {
+  *why = "";
+  if (!sp || sp->n_lines <= 0 || sp->n_lines > MC_MAX_LINES || !sp->energy_kev || !sp->weight) {
+    *why = "bad spectrum (1..512 lines)";
+    return MONTE_EINVAL;
+  }
+  const int n = sp->n_lines;
+  double wsum = 0.0;
+  for (int i = 0; i < n; i++) {
+    if (!(sp->weight[i] >= 0) || !(sp->energy_kev[i] > 0 && sp->energy_kev[i] <= 200)) {
+      *why = "spectrum lines need weight >= 0 and 0 < E <= 200 keV";
+      return MONTE_EINVAL;
+    }
+    wsum += sp->weight[i];
+  }
+  if (!(wsum > 0)) { *why = "spectrum weights sum to zero"; return MONTE_EINVAL; }
+  double q[MC_MAX_LINES];
+  int small[MC_MAX_LINES], large[MC_MAX_LINES];
+  int ns = 0, nl = 0;
+  for (int i = 0; i < n; i++) {
+    T->energy[i] = (float)sp->energy_kev[i];
+    q[i] = sp->weight[i] / wsum * n;
+    T->alias_i[i] = (int16_t)i;
+    if (q[i] < 1.0) small[ns++] = i; else large[nl++] = i;
+  }
+  while (ns > 0 && nl > 0) {
+    const int s = small[--ns], l = large[nl - 1];
+    T->alias_p[s] = (float)q[s];
+    T->alias_i[s] = (int16_t)l;
+    q[l] = (q[l] + q[s]) - 1.0;
+    if (q[l] < 1.0) {
+      nl--;
+      small[ns++] = l;
+    }
+  }
+  /* what is left is 1 up to rounding: keep the slot's own line */
+  while (nl > 0) T->alias_p[large[--nl]] = 1.0f;
+  while (ns > 0) {
+    const int s = small[--ns];
+    T->alias_p[s] = q[s] > 0.0 ? 1.0f : 0.0f;
+    if (q[s] <= 0.0) {  /* a zero-weight slot left over: give it the heaviest line */
+      int best = 0;
+      for (int i = 1; i < n; i++) if (sp->weight[i] > sp->weight[best]) best = i;
+      T->alias_i[s] = (int16_t)best;
+    }
+  }
+  T->n_lines = n;
   return MONTE_OK;
 }
 
@@ -127,23 +202,230 @@ static inline int mc_setup_tables(const monte_mc_phantom* ph, const monte_xcom* 
       T->p_photo_coh[m][k] = mu > 0.0f ? (ab + coh) / mu : 1.0f;
     }
   }
-  double wsum = 0.0;
-  for (int i = 0; i < sp->n_lines; i++) {
-    if (!(sp->weight[i] >= 0) || !(sp->energy_kev[i] > 0 && sp->energy_kev[i] <= 200)) {
-      *why = "spectrum lines need weight >= 0 and 0 < E <= 200 keV";
-      return MONTE_EINVAL;
+  return mc_setup_spectrum(sp, T, why);
+}
+
+/* Labels present in each macro cell, as 256-bit sets (4 words per cell,
+ * cell (cx, cy, cz) at ((cz mgy + cy) mgx + cx) * 4), from host labels.
+ * The library computes the same sets on the GPU for device labels. */
+static inline void mc_macro_bits_host(const monte_mc_phantom* ph, const uint8_t* labels,
+                                      const mc_params* P, uint64_t* bits) {
+  memset(bits, 0, (size_t)P->mgx * P->mgy * P->mgz * 4 * sizeof(uint64_t));
+  for (int z = 0; z < ph->nz; z++)
+    for (int y = 0; y < ph->ny; y++)
+      for (int x = 0; x < ph->nx; x++) {
+        const int l = labels[((size_t)z * ph->ny + y) * ph->nx + x];
+        const size_t c = (((size_t)(z >> P->mshift) * P->mgy + (size_t)(y >> P->mshift)) *
+                              P->mgx + (size_t)(x >> P->mshift));
+        bits[c * 4 + (l >> 6)] |= 1ull << (l & 63);
+      }
+}
+
+typedef struct {
+  float curve[MC_NBINS];
+  int id;
+} mc_class_curve;
+
+static int mc_cmp_bits4(const void* a, const void* b) {
+  return memcmp(a, b, 4 * sizeof(uint64_t));
+}
+
+static int mc_cmp_curve(const void* a, const void* b) {
+  return memcmp(((const mc_class_curve*)a)->curve, ((const mc_class_curve*)b)->curve,
+                sizeof(float) * MC_NBINS);
+}
+
+static int mc_cmp_curve_level(const void* a, const void* b) {
+  /* order by the mean majorant */
+  double sa = 0, sb = 0;
+  for (int k = 0; k < MC_NBINS; k++) {
+    sa += ((const mc_class_curve*)a)->curve[k];
+    sb += ((const mc_class_curve*)b)->curve[k];
+  }
+  return sa < sb ? -1 : (sa > sb ? 1 : 0);
+}
+
+/* Attenuation per label and bin for the local majorants: the same float
+ * products as mc_setup_tables' Woodcock tables (tables checked there). */
+static inline void mc_setup_local(const monte_mc_phantom* ph, const monte_xcom* x,
+                                  mc_local_tables* L) {
+  memset(L, 0, sizeof(*L));
+  for (int l = 0; l < ph->n_labels; l++) {
+    const int m = ph->label_material[l];
+    for (int k = 0; k < MC_NBINS; k++)
+      L->mu[l][k] = m < 0 ? 0.0f : x->total[m * MC_NBINS + k] * (float)ph->label_density[l];
+  }
+}
+
+/* Majorant classes and leg lengths (MC_F_LOCAL_MAJORANT).
+ *
+ * Class: each cell stands for itself and its 26 neighbours; its majorant
+ * curve is, bin by bin, the largest mu of any label present there (L->mu,
+ * filled by mc_setup_local).  Cells with the same curve share a class;
+ * beyond MC_MAX_CLASSES classes, classes of neighbouring levels are merged
+ * (bin-wise maxima: still majorants).
+ *
+ * Leg: the class's curve also bounds mu over the cells within Chebyshev
+ * distance R of the cell, for the largest R <= MC_MAX_LEG_CELLS such that
+ * no label above the curve lies there (found with one prefix-sum grid per
+ * class of "holds a label the class does not bound"); a photon in the cell
+ * may then move R legs of P->leg cm under that majorant.  Far from bone a
+ * leg reaches across many cells.
+ *
+ * Fills L->maj and cls[cell] = class | R << 8.  Returns MONTE_OK, or
+ * MONTE_ENOMEM. */
+#define MC_MAX_LEG_CELLS 32
+static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const uint64_t* bits,
+                                   uint16_t* cls) {
+  const int gx = P->mgx, gy = P->mgy, gz = P->mgz;
+  const size_t nc = (size_t)gx * gy * gz;
+  uint64_t* dil = (uint64_t*)malloc(nc * 5 * sizeof(uint64_t));  /* 4 words + cell index */
+  mc_class_curve* cur = (mc_class_curve*)malloc(sizeof(mc_class_curve) * (nc + 1));
+  int* set_class = (int*)malloc(sizeof(int) * nc);
+  int* set_to_class = (int*)malloc(sizeof(int) * (nc + 1));
+  int* remap = (int*)malloc(sizeof(int) * (nc + 1));
+  const size_t np = (size_t)(gx + 1) * (gy + 1) * (gz + 1);
+  int32_t* pre = (int32_t*)malloc(sizeof(int32_t) * np);
+  if (!dil || !cur || !set_class || !set_to_class || !remap || !pre) {
+    free(dil);
+    free(cur);
+    free(set_class);
+    free(set_to_class);
+    free(remap);
+    free(pre);
+    return MONTE_ENOMEM;
+  }
+  for (int z = 0; z < gz; z++)
+    for (int y = 0; y < gy; y++)
+      for (int x = 0; x < gx; x++) {
+        uint64_t w[4] = {0, 0, 0, 0};
+        for (int a = z > 0 ? z - 1 : 0; a <= (z + 1 < gz ? z + 1 : z); a++)
+          for (int b = y > 0 ? y - 1 : 0; b <= (y + 1 < gy ? y + 1 : y); b++)
+            for (int c = x > 0 ? x - 1 : 0; c <= (x + 1 < gx ? x + 1 : x); c++) {
+              const uint64_t* q = bits + (((size_t)a * gy + b) * gx + c) * 4;
+              for (int i = 0; i < 4; i++) w[i] |= q[i];
+            }
+        uint64_t* d = dil + (((size_t)z * gy + y) * gx + x) * 5;
+        memcpy(d, w, sizeof(w));
+        d[4] = ((size_t)z * gy + y) * gx + x;
+      }
+  /* distinct label sets, each with its curve */
+  qsort(dil, nc, 5 * sizeof(uint64_t), mc_cmp_bits4);
+  size_t nsets = 0;
+  for (size_t i = 0; i < nc; i++) {
+    const uint64_t* d = dil + i * 5;
+    if (i == 0 || memcmp(d, dil + (i - 1) * 5, 4 * sizeof(uint64_t)) != 0) {
+      mc_class_curve* c = &cur[nsets];
+      for (int k = 0; k < MC_NBINS; k++) c->curve[k] = 0.0f;
+      for (int l = 0; l < MC_MAX_LABELS; l++)
+        if (d[l >> 6] >> (l & 63) & 1)
+          for (int k = 0; k < MC_NBINS; k++)
+            if (L->mu[l][k] > c->curve[k]) c->curve[k] = L->mu[l][k];
+      c->id = (int)nsets;
+      nsets++;
     }
-    wsum += sp->weight[i];
+    set_class[d[4]] = (int)nsets - 1;  /* per cell: its set, for now */
   }
-  if (!(wsum > 0)) { *why = "spectrum weights sum to zero"; return MONTE_EINVAL; }
-  double acc = 0.0;
-  for (int i = 0; i < sp->n_lines; i++) {
-    acc += sp->weight[i];
-    T->cdf[i] = (float)(acc / wsum);
-    T->energy[i] = (float)sp->energy_kev[i];
+  /* sets with equal curves -> one class */
+  qsort(cur, nsets, sizeof(mc_class_curve), mc_cmp_curve);
+  int ncls = 0;
+  for (size_t i = 0; i < nsets; i++) {
+    if (i == 0 || mc_cmp_curve(&cur[i], &cur[i - 1]) != 0) {
+      if (ncls != (int)i) cur[ncls] = cur[i];
+      ncls++;
+    }
+    set_to_class[cur[i].id] = ncls - 1;
+    cur[ncls - 1].id = ncls - 1;
   }
-  T->cdf[sp->n_lines - 1] = 1.0f;
-  T->n_lines = sp->n_lines;
+  /* too many: merge runs of classes ordered by level */
+  for (int c = 0; c < ncls; c++) remap[c] = c;
+  if (ncls > MC_MAX_CLASSES) {
+    qsort(cur, ncls, sizeof(mc_class_curve), mc_cmp_curve_level);
+    mc_class_curve* merged = (mc_class_curve*)malloc(sizeof(mc_class_curve) * MC_MAX_CLASSES);
+    if (!merged) {
+      free(dil);
+      free(cur);
+      free(set_class);
+      free(set_to_class);
+      free(remap);
+      free(pre);
+      return MONTE_ENOMEM;
+    }
+    for (int g = 0; g < MC_MAX_CLASSES; g++) {
+      const int lo = (int)((long long)g * ncls / MC_MAX_CLASSES);
+      const int hi = (int)((long long)(g + 1) * ncls / MC_MAX_CLASSES);
+      for (int k = 0; k < MC_NBINS; k++) merged[g].curve[k] = 0.0f;
+      for (int c = lo; c < hi; c++) {
+        remap[cur[c].id] = g;
+        for (int k = 0; k < MC_NBINS; k++)
+          if (cur[c].curve[k] > merged[g].curve[k]) merged[g].curve[k] = cur[c].curve[k];
+      }
+    }
+    for (int g = 0; g < MC_MAX_CLASSES; g++) cur[g] = merged[g];
+    free(merged);
+    ncls = MC_MAX_CLASSES;
+  }
+  for (int c = 0; c < MC_MAX_CLASSES; c++)
+    for (int k = 0; k < MC_NBINS; k++) {
+      const float m = c < ncls ? cur[c].curve[k] : 0.0f;
+      L->maj[c][k].maj = m;
+      L->maj[c][k].inv = m > 0.0f ? 1.0f / m : 3.0e38f;
+    }
+  for (size_t i = 0; i < nc; i++) cls[i] = (uint16_t)remap[set_to_class[set_class[i]]];
+  /* leg lengths, class by class: pre = prefix sums over the grid of "the
+   * cell holds a label above the class's curve" */
+  for (int c = 0; c < ncls; c++) {
+    uint64_t bad[4] = {0, 0, 0, 0};
+    for (int l = 0; l < MC_MAX_LABELS; l++)
+      for (int k = 0; k < MC_NBINS; k++)
+        if (L->mu[l][k] > cur[c].curve[k]) {
+          bad[l >> 6] |= 1ull << (l & 63);
+          break;
+        }
+    int any = 0;
+    for (size_t i = 0; i < nc; i++) any |= (cls[i] & 0xff) == c;
+    if (!any) continue;
+#define MC_PRE(x, y, z) pre[((size_t)(z) * (gy + 1) + (size_t)(y)) * (gx + 1) + (size_t)(x)]
+    for (int z = 0; z <= gz; z++)
+      for (int y = 0; y <= gy; y++)
+        for (int x = 0; x <= gx; x++) {
+          if (!x || !y || !z) {
+            MC_PRE(x, y, z) = 0;
+            continue;
+          }
+          const uint64_t* q = bits + (((size_t)(z - 1) * gy + (y - 1)) * gx + (x - 1)) * 4;
+          const int32_t v = ((q[0] & bad[0]) | (q[1] & bad[1]) | (q[2] & bad[2]) | (q[3] & bad[3])) != 0;
+          MC_PRE(x, y, z) = v + MC_PRE(x - 1, y, z) + MC_PRE(x, y - 1, z) + MC_PRE(x, y, z - 1) -
+                            MC_PRE(x - 1, y - 1, z) - MC_PRE(x - 1, y, z - 1) -
+                            MC_PRE(x, y - 1, z - 1) + MC_PRE(x - 1, y - 1, z - 1);
+        }
+    for (int z = 0; z < gz; z++)
+      for (int y = 0; y < gy; y++)
+        for (int x = 0; x < gx; x++) {
+          const size_t i = ((size_t)z * gy + y) * gx + x;
+          if ((cls[i] & 0xff) != c) continue;
+          int r = 1;
+          while (r < MC_MAX_LEG_CELLS) {
+            const int q = r + 1;
+            const int x0 = x - q > 0 ? x - q : 0, x1 = x + q + 1 < gx ? x + q + 1 : gx;
+            const int y0 = y - q > 0 ? y - q : 0, y1 = y + q + 1 < gy ? y + q + 1 : gy;
+            const int z0 = z - q > 0 ? z - q : 0, z1 = z + q + 1 < gz ? z + q + 1 : gz;
+            const int32_t n = MC_PRE(x1, y1, z1) - MC_PRE(x0, y1, z1) - MC_PRE(x1, y0, z1) -
+                              MC_PRE(x1, y1, z0) + MC_PRE(x0, y0, z1) + MC_PRE(x0, y1, z0) +
+                              MC_PRE(x1, y0, z0) - MC_PRE(x0, y0, z0);
+            if (n) break;
+            r = q;
+          }
+          cls[i] = (uint16_t)(c | (r << 8));
+        }
+#undef MC_PRE
+  }
+  free(remap);
+  free(set_to_class);
+  free(dil);
+  free(cur);
+  free(set_class);
+  free(pre);
   return MONTE_OK;
 }
 

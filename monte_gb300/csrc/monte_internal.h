@@ -40,7 +40,11 @@ struct monte_ctx {
   monte::DevBuf fdk_views, fdk_viewsd, fdk_weights, fdk_taps, fdk_bsplit;
   // cached MC device tables
   std::vector<uint8_t> mc_key;
-  monte::DevBuf mc_tables, mc_views, mc_pixels;
+  // what the local-majorant tables in mc_mclass were built from (phantom
+  // grid, label materials and densities, attenuation tables, the cells'
+  // label sets): a call with the same key reuses them
+  std::vector<uint8_t> mc_macro_key;
+  monte::DevBuf mc_tables, mc_views, mc_pixels, mc_mclass;
   // device-side error flag word for bounded waits / kernel status
   int* d_status = nullptr;
   // autotuned backprojection tile choice, keyed by geometry

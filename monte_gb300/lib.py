@@ -59,6 +59,7 @@ def load(build_if_missing=False):
     lib.monte_fdk_last_bp_variant.argtypes = [P]
     lib.monte_fdk_last_host_ranges.argtypes = [P]
     lib.monte_fdk_set_bp_variant.argtypes = [P, C.c_int]
+    lib.monte_fdk_exact_counts.argtypes = [P, C.POINTER(C.c_uint64), C.c_int]
     lib.monte_ctx_check_status.argtypes = [P]
     MG = C.POINTER(abi.McGeom)
     lib.monte_mc_geom_reference325.argtypes = [MG]
@@ -71,6 +72,13 @@ def load(build_if_missing=False):
                                  C.POINTER(abi.McStats), C.c_int]
     lib.monte_mc_finalize.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P, P, P,
                                       P, P, P, C.c_int]
+    dp = C.POINTER(C.c_double)
+    lib.monte_spectrum_from_cumulative.argtypes = [C.POINTER(C.c_float), C.c_int32, C.c_double,
+                                                   C.c_double, dp, dp, C.POINTER(C.c_int32)]
+    lib.monte_parse_numbers.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_float), C.c_int32,
+                                        C.POINTER(C.c_int32)]
+    lib.monte_mc_sample_energies.argtypes = [P, C.POINTER(abi.McSpectrum), C.c_uint64,
+                                             C.c_uint32, C.c_uint64, P, C.c_int]
     lib.monte_batch_create.argtypes = [P, C.POINTER(abi.McXcom), C.POINTER(abi.BatchJob),
                                        C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
     lib.monte_batch_run.argtypes = [P]
@@ -122,6 +130,43 @@ def parse_xcom_csv(path_or_bytes):
     if rc != 0:
         raise MonteError(rc, "could not parse XCOM csv")
     return out
+
+
+def spectrum_from_cumulative(cum, bin_kev=0.5, fallback_kev=140.0):
+    """monte_spectrum_from_cumulative: the reference's cumulative table
+    cum[0..n_bins] -> (energies, weights) float64 lines, the fallback last.
+    Needs no GPU."""
+    lib = load()
+    cum = np.ascontiguousarray(cum, np.float32)
+    n_bins = len(cum) - 1
+    e = np.zeros(n_bins + 1, np.float64)
+    w = np.zeros(n_bins + 1, np.float64)
+    n = C.c_int32()
+    dp = C.POINTER(C.c_double)
+    rc = lib.monte_spectrum_from_cumulative(cum.ctypes.data_as(C.POINTER(C.c_float)), n_bins,
+                                            bin_kev, fallback_kev, e.ctypes.data_as(dp),
+                                            w.ctypes.data_as(dp), C.byref(n))
+    if rc != 0:
+        raise MonteError(rc, "bad cumulative spectrum table")
+    return e[:n.value], w[:n.value]
+
+
+def parse_numbers(path_or_bytes, max_values=4096):
+    """monte_parse_numbers: whitespace-separated numbers of a text table
+    (the reference's 125kv_al*.txt) -> float32 array.  Needs no GPU."""
+    lib = load()
+    if isinstance(path_or_bytes, (bytes, bytearray)):
+        data = bytes(path_or_bytes)
+    else:
+        with open(path_or_bytes, "rb") as f:
+            data = f.read()
+    out = np.zeros(max_values, np.float32)
+    n = C.c_int32()
+    rc = lib.monte_parse_numbers(data, len(data), out.ctypes.data_as(C.POINTER(C.c_float)),
+                                 max_values, C.byref(n))
+    if rc != 0:
+        raise MonteError(rc, "could not parse the table")
+    return out[:n.value].copy()
 
 
 class Context:
@@ -183,6 +228,13 @@ class Context:
         """View ranges of the last host-memory fdk() (0: it ran unpipelined)."""
         return self.lib.monte_fdk_last_host_ranges(self.h)
 
+    def fdk_exact_counts(self, reset=True):
+        """monte_fdk_exact_counts: (voxel-view pairs decided in double,
+        (column, view) weight signs taken in double) since the last reset."""
+        c = (C.c_uint64 * 2)()
+        self.check(self.lib.monte_fdk_exact_counts(self.h, c, 1 if reset else 0))
+        return int(c[0]), int(c[1])
+
     def set_bp_variant(self, variant):
         self.check(self.lib.monte_fdk_set_bp_variant(self.h, variant))
 
@@ -208,6 +260,14 @@ class Context:
                                          C.byref(request), _ptr(primary)[0], _ptr(scatter)[0],
                                          C.byref(st), mem))
         return st.as_dict()
+
+    def mc_sample_energies(self, spectrum, seed, out, job=0):
+        """monte_mc_sample_energies: source energies of histories 0..n-1 of
+        stream (seed, job) into out (float32[n])."""
+        self.check(self.lib.monte_mc_sample_energies(self.h, C.byref(spectrum), seed, job,
+                                                     out.numel() if hasattr(out, "numel")
+                                                     else out.size, _ptr(out)[0],
+                                                     _ptr(out)[1]))
 
     def mc_finalize(self, n_views, nu, nv, per, primary, scatter=None, proj0=None, map0=None,
                     proj5=None, map5=None):

@@ -99,15 +99,39 @@ def mc_run(g, inputs, request):
     request, tallies int64 [n_views][nu][nv] (labels must be host numpy)."""
     prim = np.zeros((g.n_views, g.nu, g.nv), np.int64)
     scat = np.zeros_like(prim)
-    st = (C.c_uint64 * 6)()
+    st = (C.c_uint64 * 10)()
     rc = lib().oracle_mc_run(C.byref(g), C.byref(inputs.phantom), C.byref(inputs.xcom),
                              C.byref(inputs.spectrum), C.byref(request), prim.ctypes.data,
                              scat.ctypes.data, st)
     if rc != 0:
         raise ValueError("oracle_mc_run rejected the inputs (%d)" % rc)
     names = ("histories", "woodcock_steps", "interactions", "primary_counts",
-             "scatter_counts", "dropped")
+             "scatter_counts", "dropped", "rayleigh", "compton", "photoelectric",
+             "majorant_legs")
     return prim, scat, dict(zip(names, [int(x) for x in st]))
+
+
+def mc_ref64(g, inputs, seed, per, views):
+    """The independent FP64 transport (mc_ref64.c): its own streams and
+    double arithmetic, no product code.  Returns (primary, scatter, stats)
+    for per histories at every pixel of views [views[0], views[1])."""
+    L = lib()
+    from monte_gb300 import abi
+    L.oracle_mc_ref64.argtypes = [C.POINTER(abi.McGeom), C.POINTER(abi.McPhantom),
+                                  C.POINTER(abi.McXcom), C.POINTER(abi.McSpectrum), C.c_uint64,
+                                  C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                  C.POINTER(C.c_uint64)]
+    prim = np.zeros((g.n_views, g.nu, g.nv), np.int64)
+    scat = np.zeros_like(prim)
+    st = (C.c_uint64 * 8)()
+    rc = L.oracle_mc_ref64(C.byref(g), C.byref(inputs.phantom), C.byref(inputs.xcom),
+                           C.byref(inputs.spectrum), seed, per, views[0], views[1],
+                           prim.ctypes.data, scat.ctypes.data, st)
+    if rc != 0:
+        raise ValueError("oracle_mc_ref64 rejected the inputs (%d)" % rc)
+    names = ("histories", "woodcock_steps", "interactions", "primary_counts", "scatter_counts",
+             "rayleigh", "compton", "photoelectric")
+    return prim, scat, dict(zip(names, [int(v) for v in st]))
 
 
 def stream(seed, history, job, n):

@@ -23,14 +23,21 @@
 
 typedef struct {
   uint64_t histories, steps, interactions, primary, scatter, dropped;
+  uint64_t rayleigh, compton, photo;  /* interactions by kind */
+  uint64_t legs;                      /* majorant legs (local majorants) */
 } oracle_mc_stats;
 
+/* the local-majorant tables and class grid of a run (NULL: global) */
+typedef struct {
+  const mc_local_tables* L;
+  const uint16_t* mclass;
+} oracle_local;
+
 /* One Woodcock flight: photon::delta_sampling (CBCT_real325im.cu:862-976). */
-static void fly(const mc_params* P, const mc_tables* T, const uint8_t* labels, mc_photon* p,
-                oracle_mc_stats* st) {
+static void fly(const mc_params* P, const mc_tables* T, const oracle_local* loc,
+                const uint8_t* labels, mc_photon* p, oracle_mc_stats* st) {
   while (p->state == MC_FLY) {
-    mc_flight_step(P, T, labels, p);
-    st->steps++;
+    if (mc_flight_event(P, T, loc->L, labels, loc->mclass, p)) st->steps++; else st->legs++;
     if (p->state == MC_DEAD) st->dropped++;
   }
 }
@@ -54,13 +61,14 @@ static void tally(const mc_params* P, const mc_view* V, const mc_photon* p, int6
 /* One history of `projection`: emission (:466-540), first flight (:549),
  * primary tally (:567-590), then up to max_int interactions (:599-846),
  * each followed by a flight and, on escape, a scatter tally. */
-static void history(const mc_params* P, const mc_tables* T, const mc_view* V, const mc_pixel* U,
-                    const mc_pixel* W, const uint8_t* labels, int view, int iu, int iv,
-                    uint64_t k, int64_t* prim, int64_t* scat, oracle_mc_stats* st) {
+static void history(const mc_params* P, const mc_tables* T, const oracle_local* loc,
+                    const mc_view* V, const mc_pixel* U, const mc_pixel* W,
+                    const uint8_t* labels, int view, int iu, int iv, uint64_t k, int64_t* prim,
+                    int64_t* scat, oracle_mc_stats* st) {
   mc_photon p;
   mc_start(P, T, V, U, W, view, iu, iv, k, &p);
   st->histories++;
-  fly(P, T, labels, &p, st);
+  fly(P, T, loc, labels, &p, st);
   if (p.state == MC_ESCAPED) {
     tally(P, V, &p, prim, scat, st);
     return;
@@ -68,8 +76,11 @@ static void history(const mc_params* P, const mc_tables* T, const mc_view* V, co
   for (int a = 0; a < P->max_int && p.state == MC_COLLIDED; a++) {
     p.state = mc_interact(P, T, &p);
     st->interactions++;
+    if (p.last == MC_EV_RAYLEIGH) st->rayleigh++;
+    else if (p.last == MC_EV_COMPTON) st->compton++;
+    else st->photo++;
     if (p.state != MC_FLY) return; /* photo-absorption (:651-655) */
-    fly(P, T, labels, &p, st);
+    fly(P, T, loc, labels, &p, st);
     if (p.state == MC_ESCAPED) {
       tally(P, V, &p, prim, scat, st);
       return;
@@ -95,6 +106,21 @@ int oracle_mc_run(const monte_mc_geom* g, const monte_mc_phantom* ph, const mont
   mc_pixel* W = (mc_pixel*)malloc(sizeof(mc_pixel) * g->nv);
   mc_setup_views(g, V);
   mc_setup_pixels(g, U, W);
+  oracle_local loc = {NULL, NULL};
+  mc_local_tables* L = NULL;
+  uint16_t* mclass = NULL;
+  if (P.flags & MC_F_LOCAL_MAJORANT) {
+    const size_t cells = (size_t)P.mgx * P.mgy * P.mgz;
+    uint64_t* bits = (uint64_t*)malloc(cells * 4 * sizeof(uint64_t));
+    L = (mc_local_tables*)malloc(sizeof(mc_local_tables));
+    mclass = (uint16_t*)malloc(cells * sizeof(uint16_t));
+    mc_setup_local(ph, x, L);
+    mc_macro_bits_host(ph, ph->labels, &P, bits);
+    mc_macro_classes(&P, L, bits, mclass);
+    free(bits);
+    loc.L = L;
+    loc.mclass = mclass;
+  }
   const int nvr = run->v_end - run->v_begin;
   const int npix = (run->u_end - run->u_begin) * nvr;
   oracle_mc_stats tot;
@@ -108,7 +134,7 @@ int oracle_mc_run(const monte_mc_geom* g, const monte_mc_phantom* ph, const mont
       for (int pix = 0; pix < npix; pix++) {
         int iu = run->u_begin + pix / nvr, iv = run->v_begin + pix % nvr;
         for (uint64_t k = 0; k < run->histories_per_pixel; k++)
-          history(&P, T, V, U, W, ph->labels, view, iu, iv, k, prim, scat, &st);
+          history(&P, T, &loc, V, U, W, ph->labels, view, iu, iv, k, prim, scat, &st);
       }
 #pragma omp critical
       {
@@ -118,6 +144,10 @@ int oracle_mc_run(const monte_mc_geom* g, const monte_mc_phantom* ph, const mont
         tot.primary += st.primary;
         tot.scatter += st.scatter;
         tot.dropped += st.dropped;
+        tot.rayleigh += st.rayleigh;
+        tot.compton += st.compton;
+        tot.photo += st.photo;
+        tot.legs += st.legs;
       }
     }
   }
@@ -128,7 +158,13 @@ int oracle_mc_run(const monte_mc_geom* g, const monte_mc_phantom* ph, const mont
     stats_out[3] = tot.primary;
     stats_out[4] = tot.scatter;
     stats_out[5] = tot.dropped;
+    stats_out[6] = tot.rayleigh;
+    stats_out[7] = tot.compton;
+    stats_out[8] = tot.photo;
+    stats_out[9] = tot.legs;
   }
+  free(L);
+  free(mclass);
   free(T);
   free(V);
   free(U);

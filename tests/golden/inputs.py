@@ -26,3 +26,19 @@ def fdk_projections(n_views, nu, nv, seed):
         out += (0.5 + 2.0 * amp) / (1.0 + du * du + dv * dv)
     out += 0.01 * rng.random((n_views, nu, nv))
     return out.astype(np.float32)
+
+
+def noisy_counts_map(n_views, nu, nv, histories_per_pixel, seed):
+    """A -log map like the Monte Carlo's, map[view][u][v] = ln(hpp) - ln N
+    with N Poisson counts (clamped to [1, hpp]) of hpp histories through a
+    smooth attenuation bump: pixel-to-pixel noise of ~1/sqrt(N), the case
+    where the backprojector's coordinate rounding shows in the volume.
+    Uses exp and log (libm), so it is for comparisons made on one host,
+    not for fixtures."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = (np.arange(nu, dtype=np.float64) - nu / 2) / (nu / 2)
+    b = (np.arange(nv, dtype=np.float64) - nv / 2) / (nv / 2)
+    mu = 2.0 * np.clip(1.0 - a[:, None] ** 2 - 0.5 * b[None, :] ** 2, 0.0, None)
+    n = rng.poisson(histories_per_pixel * np.exp(-mu), (n_views, nu, nv))
+    n = np.clip(n, 1, histories_per_pixel).astype(np.float64)
+    return (np.log(float(histories_per_pixel)) - np.log(n)).astype(np.float32)

@@ -75,6 +75,39 @@ def test_full_volume_against_fp64_oracle(ctx, bp_mode):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("variant", [-1, 33, 29, 0, 22, 20, 2])
+def test_noisy_maps_against_fp64_oracle(ctx, variant):
+    """Monte Carlo-like -log maps (Poisson noise, 30 histories per pixel)
+    on the batched workload's geometry for a 97^3 cube and a 256 x 256
+    detector: pixel-to-pixel noise turns any detector-coordinate error into
+    a value error one for one, so this is where the float pairs of the
+    coordinate path count (a float walk of the coordinates missed 1e-5
+    three-fold here).  Plain (-1) and tiled shapes with 32, 16, 24 and 8
+    voxels per lane, FP32 filter, 1e-5 relative RMS against the FP64
+    oracle."""
+    from inputs import noisy_counts_map
+    from monte_gb300 import batchscan
+    spec = dict(side=97, n_views=30, nu=256, nv=256)
+    g = batchscan.fdk_geom_for(spec, batchscan.mc_geom_for(spec))
+    proj = noisy_counts_map(g.n_views, g.nu, g.nv, 30, 97)
+    f64 = oracle.fdk_filter(g, proj, precise=True)
+    v64 = oracle.fdk_backproject(g, f64)
+    p = torch.from_numpy(proj).cuda()
+    xy = torch.empty((g.nz, g.ny, g.nx), device="cuda")
+    try:
+        if variant >= 0:
+            ctx.set_bp_variant(variant)
+        bm = abi.MONTE_BP_PLAIN if variant < 0 else abi.MONTE_BP_TILED
+        ctx.fdk(g, p, xy, filter_mode=abi.MONTE_FILTER_FP32, bp_mode=bm)
+        ctx.check_status()
+        if variant >= 0:
+            assert ctx.last_bp_variant() == variant
+    finally:
+        ctx.set_bp_variant(-1)
+    err = rel_rms(xy.cpu().numpy(), v64)
+    assert err < 1e-5, (variant, err)
+
+
 def test_host_memory_path_equals_device_path(ctx):
     g = abi.fdk_geom_reference65()
     proj = fdk_projections(360, 65, 65, 11)

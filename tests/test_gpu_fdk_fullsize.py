@@ -8,10 +8,13 @@ the size.
   the same filtered projections: 1e-5 relative RMS;
 * the FP64 oracle filter on four views: 1e-5 for the FP32 and the
   tensor-core filter;
-* the leading tile shapes, which all group 32 voxels per lane along z,
-  give the same volume bit for bit; the shared-ring shape 0 (16 voxels per
-  lane) agrees with them to FP32 rounding, as each group walks its row
-  coordinates from its own first voxel;
+* the benchmark's own chain -- the tensor-core filter, the autotuned tile
+  shape, the volume -- against the FP64 oracle (FP64 filter of all 360
+  views, FP64 backprojection) on those nine slices: 1e-5;
+* tile shapes that take 16, 32 or 64 voxels per lane give the same volume
+  bit for bit (their row anchors sit at the same multiples of 16 in z),
+  per-warp and shared-ring kernels alike; shapes with 24 voxels per lane
+  (anchors every 8) agree with them to FP32 rounding;
 * the pinned host pipeline (three view ranges) equals the device path bit
   for bit;
 * linearity, FDK(a p + b q) = a FDK(p) + b FDK(q): 1e-5 (FP32 rounding)."""
@@ -57,6 +60,19 @@ def test_full_size_slices_against_oracle(ctx, scan):
         assert err < 1e-5, (z0, err)
 
 
+def test_full_size_benchmark_chain_against_fp64_oracle(ctx, scan):
+    g, proj = scan
+    best = ctx.fdk_autotune(g)
+    _, xy = _fdk(ctx, g, proj, abi.MONTE_FILTER_BF16X3)
+    assert ctx.last_bp_variant() == best
+    f64 = oracle.fdk_filter(g, proj.cpu().numpy(), precise=True)
+    xyh = xy.cpu().numpy()
+    for z0, z1 in SLABS:
+        ref = oracle.fdk_backproject(g, f64, z_range=(z0, z1))
+        err = rel_rms(xyh[z0:z1], ref[z0:z1])
+        assert err < 1e-5, (z0, err)
+
+
 def test_full_size_filters_against_fp64_oracle(ctx, scan):
     g, proj = scan
     views = [0, 97, 211, 359]
@@ -74,7 +90,7 @@ def test_full_size_tile_shapes_agree(ctx, scan):
     f, _ = _fdk(ctx, g, proj)
     ref = None
     try:
-        for variant in (33, 29, 30, 24, 0):
+        for variant in (33, 29, 30, 24, 0, 22, 31, 20):
             ctx.set_bp_variant(variant)
             xy = torch.empty((g.nz, g.ny, g.nx), device="cuda")
             ctx.fdk_backproject(g, f, xy, mode=abi.MONTE_BP_TILED)
@@ -82,7 +98,7 @@ def test_full_size_tile_shapes_agree(ctx, scan):
             assert ctx.last_bp_variant() == variant
             if ref is None:
                 ref = xy
-            if variant != 0:
+            if variant != 20:
                 assert torch.equal(xy, ref), variant
             else:
                 err = rel_rms(xy.cpu().numpy(), ref.cpu().numpy())

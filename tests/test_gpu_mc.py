@@ -48,7 +48,8 @@ def _gpu_run(ctx, g, inp_dev, req):
 
 @pytest.mark.parametrize("spectrum", ["mono", "poly"])
 @pytest.mark.parametrize("flags", [abi.MONTE_MC_STALE_SIN_PHI, 0,
-                                   abi.MONTE_MC_FIRST_COMPTON_Z | abi.MONTE_MC_NO_RAYLEIGH_TALLY])
+                                   abi.MONTE_MC_FIRST_COMPTON_Z | abi.MONTE_MC_NO_RAYLEIGH_TALLY,
+                                   abi.MONTE_MC_STALE_SIN_PHI | abi.MONTE_MC_LOCAL_MAJORANT])
 def test_replay_is_bit_exact(ctx, spectrum, flags):
     g = cfg1_geom(flags)
     host = cfg1_inputs(None, spectrum)
@@ -64,6 +65,11 @@ def test_replay_is_bit_exact(ctx, spectrum, flags):
         assert st["histories"] == st_ref["histories"]
         assert st["woodcock_steps"] == st_ref["woodcock_steps"]
         assert st["interactions"] == st_ref["interactions"]
+        for kind in ("rayleigh", "compton", "photoelectric"):
+            assert st[kind] == st_ref[kind], (kernel, kind)
+        assert st["rayleigh"] + st["compton"] + st["photoelectric"] == st["interactions"]
+        assert st["majorant_legs"] == st_ref["majorant_legs"]
+        assert (st["majorant_legs"] > 0) == bool(flags & abi.MONTE_MC_LOCAL_MAJORANT)
 
 
 def test_split_runs_sum_to_the_whole(ctx):

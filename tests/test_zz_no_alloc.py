@@ -79,3 +79,63 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
                                   p.data_ptr(), p.data_ptr(), None, None)
     assert rc == abi.MONTE_EINVAL
     assert b"static scratch" in lib.monte_last_error(None)
+
+
+def test_noalloc_back_to_back_without_sync_and_plain_kernel(ctx):
+    """Two calls queued on one stream with no statistics (so no wait in
+    between: the second call's tables overwrite the shared array while the
+    first kernel may still be queued -- stream order keeps them apart),
+    then one synchronize; the plain kernel as well as the persistent one."""
+    lib = load()
+    inp = _inputs()
+    g = abi.mc_geom(90, 64, 64, 0.1, 50.0, 100.0, 3.5, flags=abi.MONTE_MC_STALE_SIN_PHI)
+    lib.monte_mc_run_noalloc.argtypes = [C.POINTER(abi.McGeom), C.POINTER(abi.McPhantom),
+                                         C.POINTER(abi.McXcom), C.POINTER(abi.McSpectrum),
+                                         C.POINTER(abi.McRequest), C.c_void_p, C.c_void_p,
+                                         C.POINTER(abi.McStats), C.c_void_p]
+    requests = [abi.mc_request(303, 4, (2, 4), (0, 64), (0, 64), abi.MONTE_MC_PLAIN),
+                abi.mc_request(404, 2, (5, 8), (8, 56), (4, 60), abi.MONTE_MC_PERSISTENT)]
+    outs = []
+    stream = torch.cuda.current_stream().cuda_stream
+    for req in requests:
+        p = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device="cuda")
+        s = torch.zeros_like(p)
+        rc = lib.monte_mc_run_noalloc(C.byref(g), C.byref(inp.phantom), C.byref(inp.xcom),
+                                      C.byref(inp.spectrum), C.byref(req), p.data_ptr(),
+                                      s.data_ptr(), None, C.c_void_p(stream))
+        assert rc == 0, lib.monte_last_error(None)
+        outs.append((p, s))
+    torch.cuda.synchronize()
+    for req, (p, s) in zip(requests, outs):
+        p0 = torch.zeros_like(p)
+        s0 = torch.zeros_like(p)
+        ctx.mc_run(g, inp, req, p0, s0)
+        torch.cuda.synchronize()
+        assert torch.equal(p, p0) and torch.equal(s, s0), req.kernel
+
+
+def test_noalloc_rejects_host_pointers_and_capture():
+    lib = load()
+    inp = _inputs()
+    g = abi.mc_geom(90, 64, 64, 0.1, 50.0, 100.0, 3.5, flags=abi.MONTE_MC_STALE_SIN_PHI)
+    req = abi.mc_request(5, 1, (0, 1), (0, 64), (0, 64))
+    lib.monte_mc_run_noalloc.argtypes = [C.POINTER(abi.McGeom), C.POINTER(abi.McPhantom),
+                                         C.POINTER(abi.McXcom), C.POINTER(abi.McSpectrum),
+                                         C.POINTER(abi.McRequest), C.c_void_p, C.c_void_p,
+                                         C.POINTER(abi.McStats), C.c_void_p]
+    host = np.zeros((g.n_views, g.nu, g.nv), np.int64)
+    dev = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device="cuda")
+    rc = lib.monte_mc_run_noalloc(C.byref(g), C.byref(inp.phantom), C.byref(inp.xcom),
+                                  C.byref(inp.spectrum), C.byref(req), host.ctypes.data,
+                                  dev.data_ptr(), None, None)
+    assert rc == abi.MONTE_EINVAL
+    # a capturing stream: refused before any work is issued
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        graph.capture_begin(capture_error_mode="relaxed")
+        rc = lib.monte_mc_run_noalloc(C.byref(g), C.byref(inp.phantom), C.byref(inp.xcom),
+                                      C.byref(inp.spectrum), C.byref(req), dev.data_ptr(),
+                                      dev.data_ptr(), None, C.c_void_p(s.cuda_stream))
+        graph.capture_end()
+    assert rc == abi.MONTE_EUNSUPPORTED
