@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--tile", type=int, default=-1,
                     help="backprojection tile shape (default: autotune)")
     ap.add_argument("--small", action="store_true", help="reduced sizes (for profiling runs)")
+    ap.add_argument("--mc-case", action="store_true",
+                    help="only run one view of the Monte Carlo workload at 16 histories per "
+                         "pixel, once per transport (the case profiled with ncu), and exit")
     return ap.parse_args()
 
 
@@ -245,9 +248,21 @@ def mc_cpu_baseline(g, inp, per=256):
                       "(%d histories, %.1f s)" % (per, st["histories"], dt)}
 
 
+# Warp instructions per history and active lanes per issued instruction of
+# the persistent kernel on this workload, from one ncu capture of one view
+# at 16 histories per pixel per transport (`bench.py --mc-case` under ncu
+# with smsp__inst_executed.sum and smsp__thread_inst_executed.sum: 3,145,728
+# histories per launch), for the issue roofline of the Monte Carlo line.
+MC_PROFILE = {"global": {"warp_inst_per_history": 503.8, "lanes_per_instruction": 16.58},
+              "local": {"warp_inst_per_history": 314.3, "lanes_per_instruction": 11.43}}
+
+
 def mc_bench(ctx, device, steps=3, per=509, with_cpu=True):
-    """Histories/s of the persistent and the plain Monte Carlo kernels on one
-    view of the 325^3 workload (1.0e8 histories per step)."""
+    """Histories/s on one view of the 325^3 workload (1.0e8 histories per
+    step) in three forms: the plain kernel with the reference's single
+    majorant (the one-instance form), the persistent kernel with it, and
+    the persistent kernel with local majorants (MONTE_MC_LOCAL_MAJORANT, the
+    headline)."""
     import torch
     from monte_gb300 import abi
     g, lab, make = mc_workload()
@@ -256,25 +271,65 @@ def mc_bench(ctx, device, steps=3, per=509, with_cpu=True):
     scat = torch.zeros_like(prim)
     out = {"metric": "MC histories/s", "unit": "histories/s", "workload": MC_WORKLOAD}
     stream = torch.cuda.current_stream(device)
-    for name, kernel in (("persistent", abi.MONTE_MC_PERSISTENT), ("plain", abi.MONTE_MC_PLAIN)):
+    forms = (("persistent_local", abi.MONTE_MC_PERSISTENT, abi.MONTE_MC_LOCAL_MAJORANT),
+             ("persistent", abi.MONTE_MC_PERSISTENT, 0),
+             ("plain", abi.MONTE_MC_PLAIN, 0))
+    for name, kernel, extra in forms:
+        g.flags = abi.MONTE_MC_STALE_SIN_PHI | extra
         req = abi.mc_request(2024, per, (0, 1), (0, g.nu), (0, g.nv), kernel)
-        st = ctx.mc_run(g, inp, req, prim, scat)  # warm-up
+        st = ctx.mc_run(g, inp, req, prim, scat)  # warm-up (builds the local tables)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(device)
         e0.record(stream)
         for i in range(steps):
             req.view_begin, req.view_end = 1 + i, 2 + i
-            ctx.mc_run(g, inp, req, prim, scat)
+            st = ctx.mc_run(g, inp, req, prim, scat)
         e1.record(stream)
         torch.cuda.synchronize(device)
         dt = e0.elapsed_time(e1) / 1e3
         hist = steps * per * g.nu * g.nv
+        h = st["histories"]
         out[name] = {"value": hist / dt, "ms_per_view": dt / steps * 1e3,
-                     "woodcock_steps_per_history": st["woodcock_steps"] / st["histories"],
-                     "interactions_per_history": st["interactions"] / st["histories"]}
-    out["value"] = out["persistent"]["value"]
-    out["persistent_over_plain"] = out["persistent"]["value"] / out["plain"]["value"]
+                     "woodcock_steps_per_history": st["woodcock_steps"] / h,
+                     "majorant_legs_per_history": st["majorant_legs"] / h,
+                     "interactions_per_history": st["interactions"] / h,
+                     "rayleigh_compton_photo": [st["rayleigh"], st["compton"],
+                                                st["photoelectric"]]}
+    g.flags = abi.MONTE_MC_STALE_SIN_PHI
+    best = out["persistent_local"]
+    out["value"] = best["value"]
+    out["persistent_over_plain"] = best["value"] / out["plain"]["value"]
+    out["local_over_global_majorant"] = best["value"] / out["persistent"]["value"]
+    # roofline: every event (Woodcock step, majorant leg, interaction) reads
+    # one 32-byte sector (a label, a class cell or a table row) and every
+    # history adds one 8-byte tally; the 34 MB label volume stays in L2
+    ev = (best["woodcock_steps_per_history"] + best["majorant_legs_per_history"] +
+          best["interactions_per_history"])
+    bytes_per_hist = 32.0 * ev + 8.0
+    out["roofline_l2"] = {"kernel": "mc_persistent_kernel", "bound": "l2",
+                          "algorithmic_bytes_per_history": bytes_per_hist,
+                          "achieved": bytes_per_hist * best["value"] / 1e9, "unit": "GB/s",
+                          "note": "label gathers hit L2; no measured L2 peak in "
+                                  "MEASURED_PEAKS.json, so no fraction"}
+    prof = MC_PROFILE.get("local")
+    if prof:
+        peaks = {}
+        try:
+            with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except OSError:
+            pass
+        clk = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+        n_sm = torch.cuda.get_device_properties(device).multi_processor_count
+        peak = n_sm * 4 * clk / 1e12  # warp instructions per second, in T/s
+        ach = prof["warp_inst_per_history"] * best["value"] / 1e12
+        out["roofline"] = {"kernel": "mc_persistent_kernel", "bound": "issue",
+                           "achieved": ach, "peak": peak, "unit": "T warp-instructions/s",
+                           "frac": ach / peak,
+                           "warp_inst_per_history": prof["warp_inst_per_history"],
+                           "lanes_per_instruction": prof["lanes_per_instruction"],
+                           "peak_source": "%d SMs x 4 schedulers x %.0f MHz" % (n_sm, clk / 1e6)}
     if with_cpu:
         out["cpu_baseline"] = mc_cpu_baseline(g, make(lab))
     return out
@@ -507,6 +562,17 @@ def run_ours(args):
     ms_per_step = elapsed / args.steps * 1e3
     value = world * updates * args.steps / elapsed / 1e9
 
+    # how much of one backprojection left FP32: voxel-view pairs decided in
+    # double next to the operator's discontinuities, weight signs in double
+    exact = None
+    if bmode == abi.MONTE_BP_TILED:
+        ctx.fdk_exact_counts(reset=True)
+        ctx.fdk_backproject(g, filt, vol, mode=bmode)
+        n_pairs, n_signs = ctx.fdk_exact_counts(reset=True)
+        n_cols = g.nx * g.ny * g.n_views
+        exact = {"voxel_view_pairs_in_double": n_pairs, "share_of_updates": n_pairs / updates,
+                 "weight_signs_in_double": n_signs, "share_of_column_views": n_signs / n_cols}
+
     # end to end through the C ABI with pinned host buffers
     h_proj = proj.cpu().pin_memory()
     h_vol = torch.empty((g.nz, g.ny, g.nx), dtype=torch.float32).pin_memory()
@@ -536,8 +602,8 @@ def run_ours(args):
     bp_bytes = g.n_views * g.nu * g.nv * 4 + g.nx * g.ny * g.nz * 4
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     # DRAM bytes (read + write) of one backprojection launch of this workload,
-    # from ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) for the
-    # tile shapes that lead it; profiles/bp_warp_recon325.md gives the command
+    # from one-pass ncu captures (dram__bytes_read.sum + dram__bytes_write.sum)
+    # of the tile shapes that lead it
     traffic = BP_TRAFFIC.get(ctx.last_bp_variant()) if not args.small else None
 
     line = {
@@ -566,6 +632,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(g.nx * g.ny * g.nz * 4),
                 "pipeline_view_ranges": e2e_ranges},
         "gpu_launches": 2 * args.steps,
+        "exact_path": exact,
         "clocks": clk,
     }
     # the plain one-instance FP32 form of the same FDK (FP32 filter, one voxel
@@ -589,7 +656,7 @@ def run_ours(args):
                              "tuned_over_plain": value / world / (updates / t_plain / 1e9)}
     if not args.no_mc:
         line["mc"] = mc_bench(ctx, dev, with_cpu=rank == 0 and not args.no_cpu_baseline)
-        line["gpu_launches_mc"] = 2 * 4
+        line["gpu_launches_mc"] = 3 * 4
     if not args.no_batch and not args.small:
         line["batch"] = batch_bench(ctx, dev, args.batch_scale)
     if not args.no_diff and not args.small:
@@ -604,8 +671,31 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def mc_case():
+    """One view of the 325^3 Monte Carlo workload at 16 histories per pixel
+    with the single majorant, then with local majorants: two launches of the
+    persistent kernel, small enough to capture with ncu."""
+    import torch
+    from monte_gb300 import abi
+    from monte_gb300.lib import Context
+    g, lab, make = mc_workload()
+    inp = make(torch.from_numpy(lab).cuda())
+    ctx = Context(0, stream=torch.cuda.current_stream())
+    for extra in (0, abi.MONTE_MC_LOCAL_MAJORANT):
+        g.flags = abi.MONTE_MC_STALE_SIN_PHI | extra
+        prim = torch.zeros((g.n_views, g.nu, g.nv), dtype=torch.int64, device="cuda")
+        scat = torch.zeros_like(prim)
+        st = ctx.mc_run(g, inp, abi.mc_request(2024, 16, (0, 1), (0, g.nu), (0, g.nv)), prim, scat)
+        torch.cuda.synchronize()
+        print(json.dumps({"flags": g.flags, "stats": st}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.mc_case:
+        mc_case()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -287,12 +287,14 @@ MONTE_HD void mc_flight_step(const mc_params* P, const mc_tables* T, const uint8
  * delta tracking with a piecewise-constant majorant.  The photon carries
  * tau, the optical depth left of its current exponential draw.  In the
  * macro cell holding it, the majorant m of the cell's class bounds mu over
- * the cell and its 26 neighbours, so over the next `leg` cm at least.  If
- * tau / m fits in a leg the photon moves there and makes a tentative
- * collision, accepted with probability mu(label) / m (a Woodcock step);
- * otherwise it moves one leg and spends m * leg of tau (nothing can
- * collide there beyond what m accounts for; exponential flights are
- * memoryless).  Air-only cells (m = 0) are crossed a leg at a time.
+ * every cell within R cells of it (R >= 1 is stored with the class), so
+ * over the next R legs of P->leg cm at least: a leg is shorter than a
+ * cell's smallest edge.  If tau / m fits in those R legs the photon moves
+ * there and makes a tentative collision, accepted with probability
+ * mu(label) / m (a Woodcock step); otherwise it moves the R legs and
+ * spends m times their length of tau (nothing can collide there beyond
+ * what m accounts for; exponential flights are memoryless).  Air-only
+ * cells (m = 0) are crossed R legs at a time.
  * Returns 1 after a tentative collision, 0 after a leg; updates p->state. */
 MONTE_HD int mc_flight_leg(const mc_params* P, const mc_local_tables* L, const uint8_t* labels,
                            const uint16_t* mclass, mc_photon* p) {

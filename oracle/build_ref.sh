@@ -15,8 +15,10 @@
 # monte_cpp/CBCT_real2.cpp:16,614);
 # with FORTIFY the default Ubuntu build aborts after computing.
 set -euo pipefail
-REF=${MONTE_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+# the reference tree: MONTE_REFERENCE, else a "reference" directory beside
+# the repository
+REF=${MONTE_REFERENCE:-$(dirname "$(dirname "$HERE")")/reference}
 OUT="$HERE/_ref"
 if [ ! -d "$REF/recon" ]; then
   echo "reference tree not found at $REF; nothing to build" >&2

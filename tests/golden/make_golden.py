@@ -33,7 +33,9 @@ sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 from inputs import fdk_projections  # noqa: E402
 
-REF = os.environ.get("MONTE_REFERENCE", "/root/reference")
+# the reference tree: MONTE_REFERENCE, else a "reference" directory beside
+# the repository
+REF = os.environ.get("MONTE_REFERENCE", os.path.join(os.path.dirname(REPO), "reference"))
 BIN = os.path.join(REPO, "oracle", "_ref")
 
 

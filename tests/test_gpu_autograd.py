@@ -3,7 +3,7 @@ thin Functions over the C ABI's forward and backward entry points).
 Gradients that autograd assembles from the library's adjoints are checked
 against the FP64 oracle's gradients and against central finite differences
 of the FP64 oracle loss; the recomputing least-squares op equals the plain
-composition bit for bit."""
+composition to rounding."""
 import numpy as np
 import pytest
 import torch
@@ -38,11 +38,15 @@ def test_least_squares_gradient_through_autograd(ctx):
         g, oracle.fdk_forward_project(g, x64.astype(np.float32).astype(np.float64)) - p64)
     assert rel_rms(g_auto.cpu().numpy(), g64) < 1e-4
     # the recomputing op: the same gradient, nothing projection-sized kept
+    # between forward and backward.  Equal to rounding, not bit for bit: its
+    # residual is formed in float rather than double, and the forward
+    # projector accumulates detector pixels with atomics, so two runs of A x
+    # differ in summation order.
     x.grad = None
     loss2 = LeastSquares.apply(x, p, ctx, g)
     loss2.backward()
-    assert torch.equal(x.grad, g_auto)
-    assert abs(float(loss2) - float(loss)) <= 1e-12 * abs(float(loss))
+    assert rel_rms(x.grad.cpu().numpy(), g_auto.cpu().numpy()) < 1e-6
+    assert abs(float(loss2) - float(loss)) <= 1e-7 * abs(float(loss))
 
 
 def test_least_squares_central_differences(ctx):

@@ -19,7 +19,8 @@ from monte_gb300 import abi, phantoms
 def test_xcom_parser_matches_fixture():
     from monte_gb300.lib import parse_xcom_csv
     import os
-    ref = os.environ.get("MONTE_REFERENCE", "/root/reference")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    ref = os.environ.get("MONTE_REFERENCE", os.path.join(os.path.dirname(repo), "reference"))
     path = os.path.join(ref, "monte_cpp", "xcom2.csv")
     x = golden("xcom")
     if not os.path.exists(path):
