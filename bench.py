@@ -253,8 +253,8 @@ def mc_cpu_baseline(g, inp, per=256):
 # at 16 histories per pixel per transport (`bench.py --mc-case` under ncu
 # with smsp__inst_executed.sum and smsp__thread_inst_executed.sum: 3,145,728
 # histories per launch), for the issue roofline of the Monte Carlo line.
-MC_PROFILE = {"global": {"warp_inst_per_history": 503.8, "lanes_per_instruction": 16.58},
-              "local": {"warp_inst_per_history": 314.3, "lanes_per_instruction": 11.43}}
+MC_PROFILE = {"global": {"warp_inst_per_history": 520.0, "lanes_per_instruction": 17.90},
+              "local": {"warp_inst_per_history": 240.9, "lanes_per_instruction": 12.40}}
 
 
 def mc_bench(ctx, device, steps=3, per=509, with_cpu=True):
@@ -587,7 +587,22 @@ def run_ours(args):
     t_e2e = max_over_ranks(t_e2e, world, dev)
     e2e_val = world * updates * n_e2e / t_e2e / 1e9
     e2e_ranges = ctx.last_host_ranges()
-    del h_vol
+    # the host link's rates on this machine, one pinned copy each way of the
+    # same buffers (the end-to-end figure follows them: only the first
+    # view range's upload and the last range's volume store are exposed)
+    d_tmp = torch.empty_like(proj)
+    h2d, d2h = [], []
+    for _ in range(3):
+        c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        c0.record()
+        d_tmp.copy_(h_proj, non_blocking=True)
+        c1.record()
+        h_vol.copy_(vol, non_blocking=True)
+        c2.record()
+        c2.synchronize()
+        h2d.append(h_proj.numel() * 4 / (c0.elapsed_time(c1) / 1e3) / 1e9)
+        d2h.append(h_vol.numel() * 4 / (c1.elapsed_time(c2) / 1e3) / 1e9)
+    del d_tmp, h_vol
 
     peaks = {}
     try:
@@ -630,7 +645,8 @@ def run_ours(args):
         "e2e": {"value": e2e_val, "unit": "GUPS",
                 "h2d_bytes_per_step": int(g.n_views * g.nu * g.nv * 4),
                 "d2h_bytes_per_step": int(g.nx * g.ny * g.nz * 4),
-                "pipeline_view_ranges": e2e_ranges},
+                "pipeline_view_ranges": e2e_ranges, "fraction_of_value": e2e_val / value,
+                "h2d_gbs": statistics.median(h2d), "d2h_gbs": statistics.median(d2h)},
         "gpu_launches": 2 * args.steps,
         "exact_path": exact,
         "clocks": clk,

@@ -68,6 +68,7 @@ struct monte_batch {
   monte::DevBuf arena;
   size_t o_mcdev = 0, o_starts = 0, o_counters = 0;
   unsigned long long total = 0;
+  bool mc_all_local = false;               // every job uses MONTE_MC_LOCAL_MAJORANT
   unsigned long long* counters = nullptr;  // [0] batch counter, [4..13] stats, [16+j] per job
   cudaStream_t lanes[monte::kLanes] = {};
   cudaEvent_t fork = nullptr;
@@ -184,7 +185,7 @@ int capture(monte_batch* B) {
     unsigned char* base = (unsigned char*)B->arena.ptr;
     e = launch_mc_batch((const McDev*)(base + B->o_mcdev),
                         (const unsigned long long*)(base + B->o_starts), n, B->total, B->counters,
-                        B->counters + 4, ctx->sm_count, s0);
+                        B->counters + 4, B->mc_all_local, ctx->sm_count, s0);
     if (e != cudaSuccess) return fail(cuda_fail(ctx, e, "batch Monte Carlo launch"));
   }
   e = cudaEventRecord(B->fork, s0);
@@ -322,6 +323,9 @@ int create_plan(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* j
     starts[j + 1] = starts[j] + b.histories;
   }
   B->total = starts[n];
+  B->mc_all_local = true;
+  for (int j = 0; j < n; j++)
+    B->mc_all_local = B->mc_all_local && (B->jobs[j].job.mc.flags & MONTE_MC_LOCAL_MAJORANT);
   MONTE_TRY(upload(ctx, devs.data(), base + B->o_mcdev, devs.size() * sizeof(McDev)));
   MONTE_TRY(upload(ctx, starts.data(), base + B->o_starts, starts.size() * sizeof(unsigned long long)));
   MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -49,9 +49,12 @@ cudaError_t launch_mc(const McDev& d, int kernel, int sm_count, cudaStream_t st)
 constexpr int kMaxBatchJobs = 1024;
 // One persistent launch over the histories of n_jobs jobs; starts[j] is the
 // first global history of job j, starts[n_jobs] = total (device arrays).
+// all_local: every job tracks with local majorants (the shorter rounds of
+// that transport).
 cudaError_t launch_mc_batch(const McDev* jobs, const unsigned long long* starts, int n_jobs,
                             unsigned long long total, unsigned long long* counter,
-                            unsigned long long* stats, int sm_count, cudaStream_t st);
+                            unsigned long long* stats, bool all_local, int sm_count,
+                            cudaStream_t st);
 // Labels present in each macro cell of the local majorants (mc_setup.h's
 // mc_macro_bits_host, for labels in device memory): 4 words per cell.
 cudaError_t launch_mc_macro_bits(const uint8_t* labels, const mc_params& P, unsigned long long* bits,

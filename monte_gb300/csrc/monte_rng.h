@@ -102,6 +102,11 @@ typedef struct {
   uint32_t job;
   uint32_t next;        /* index of the next draw */
   uint32_t buf[4];      /* outputs of block next/4 (valid when next%4 != 0) */
+  uint32_t pf;          /* device kernels only: shared-memory byte address of a
+                           16-byte slot that monte_stream_prefetch fills with
+                           the block the next wrap of `next` loads, bit 0 set
+                           while it holds it; 0 = no slot (the host, and kernels
+                           that do not prefetch) */
 } monte_stream;
 
 MONTE_HD void monte_stream_init(monte_stream* s, uint64_t seed, uint64_t history, uint32_t job) {
@@ -112,6 +117,7 @@ MONTE_HD void monte_stream_init(monte_stream* s, uint64_t seed, uint64_t history
   s->job = job;
   s->next = 0;
   s->buf[0] = s->buf[1] = s->buf[2] = s->buf[3] = 0;
+  s->pf = 0;
 }
 
 MONTE_HD uint32_t monte_stream_u32(monte_stream* s) {
@@ -138,6 +144,14 @@ MONTE_HD uint32_t monte_stream_u32(monte_stream* s) {
  * schedule of the stream's key). */
 MONTE_HD uint32_t monte_stream_u32_keys(monte_stream* s, const monte_philox_keys* K) {
   uint32_t w = s->next & 3u;
+#if defined(__CUDA_ARCH__)
+  if (w == 0 && (s->pf & 1u)) {  /* the block was prefetched */
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(s->buf[0]), "=r"(s->buf[1]), "=r"(s->buf[2]), "=r"(s->buf[3])
+                 : "r"(s->pf & ~15u));
+    s->pf &= ~1u;
+  } else
+#endif
   if (w == 0) {
     monte_u32x4 c;
     c.v[0] = s->next >> 2;
@@ -153,6 +167,30 @@ MONTE_HD uint32_t monte_stream_u32_keys(monte_stream* s, const monte_philox_keys
   s->next++;
   return w == 0 ? s->buf[0] : w == 1 ? s->buf[1] : w == 2 ? s->buf[2] : s->buf[3];
 }
+
+#if defined(__CUDACC__)
+/* Compute, ahead of need, the block that the next wrap of s->next loads
+ * (block next/4 when next%4 == 0, else the one after it) into the stream's
+ * shared-memory slot.  The draws are the same whenever the block is
+ * computed; what changes is where the Philox rounds run.  A warp runs a
+ * divergent branch once for all of its lanes that take it, so a kernel
+ * whose lanes draw at their own pace would run the ten rounds in nearly
+ * every step for the few lanes whose block ran out; prefetching for every
+ * lane without a block whenever one lane is about to run out makes those
+ * passes several steps apart. */
+__device__ __forceinline__ void monte_stream_prefetch(monte_stream* s, const monte_philox_keys* K) {
+  monte_u32x4 c;
+  c.v[0] = (s->next + 3u) >> 2;
+  c.v[1] = s->h_lo;
+  c.v[2] = s->h_hi;
+  c.v[3] = s->job;
+  const monte_u32x4 r = monte_philox4x32_10_keys(c, K);
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(s->pf & ~15u), "r"(r.v[0]),
+               "r"(r.v[1]), "r"(r.v[2]), "r"(r.v[3])
+               : "memory");
+  s->pf |= 1u;
+}
+#endif
 
 /* Uniform on (0, 1] with 24-bit resolution, like curand_uniform's range
  * (the reference's -log(beta) needs beta > 0, CBCT_real325im.cu:888-889). */
