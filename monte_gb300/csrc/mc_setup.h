@@ -228,10 +228,6 @@ typedef struct {
   int id;
 } mc_class_curve;
 
-static int mc_cmp_bits4(const void* a, const void* b) {
-  return memcmp(a, b, 4 * sizeof(uint64_t));
-}
-
 static int mc_cmp_curve(const void* a, const void* b) {
   return memcmp(((const mc_class_curve*)a)->curve, ((const mc_class_curve*)b)->curve,
                 sizeof(float) * MC_NBINS);
@@ -281,25 +277,24 @@ static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const
                                    uint16_t* cls) {
   const int gx = P->mgx, gy = P->mgy, gz = P->mgz;
   const size_t nc = (size_t)gx * gy * gz;
-  uint64_t* dil = (uint64_t*)malloc(nc * 5 * sizeof(uint64_t));  /* 4 words + cell index */
-  mc_class_curve* cur = (mc_class_curve*)malloc(sizeof(mc_class_curve) * (nc + 1));
+  /* distinct dilated label sets, found by open addressing on their four
+   * words (set ids in order of first appearance), each with its curve */
+  size_t cap = 64;
+  while (cap < 2 * nc) cap <<= 1;
+  size_t ucap = 64, nsets = 0;
+  int32_t* table = (int32_t*)malloc(sizeof(int32_t) * cap);
+  uint64_t* uniq = (uint64_t*)malloc(ucap * 4 * sizeof(uint64_t));
+  mc_class_curve* cur = (mc_class_curve*)malloc(sizeof(mc_class_curve) * ucap);
   int* set_class = (int*)malloc(sizeof(int) * nc);
   int* set_to_class = (int*)malloc(sizeof(int) * (nc + 1));
   int* remap = (int*)malloc(sizeof(int) * (nc + 1));
   const size_t np = (size_t)(gx + 1) * (gy + 1) * (gz + 1);
   int32_t* pre = (int32_t*)malloc(sizeof(int32_t) * np);
-  if (!dil || !cur || !set_class || !set_to_class || !remap || !pre) {
-    free(dil);
-    free(cur);
-    free(set_class);
-    free(set_to_class);
-    free(remap);
-    free(pre);
-    return MONTE_ENOMEM;
-  }
-  for (int z = 0; z < gz; z++)
-    for (int y = 0; y < gy; y++)
-      for (int x = 0; x < gx; x++) {
+  int oom = !table || !uniq || !cur || !set_class || !set_to_class || !remap || !pre;
+  if (!oom) memset(table, 0xff, sizeof(int32_t) * cap);
+  for (int z = 0; z < gz && !oom; z++)
+    for (int y = 0; y < gy && !oom; y++)
+      for (int x = 0; x < gx && !oom; x++) {
         uint64_t w[4] = {0, 0, 0, 0};
         for (int a = z > 0 ? z - 1 : 0; a <= (z + 1 < gz ? z + 1 : z); a++)
           for (int b = y > 0 ? y - 1 : 0; b <= (y + 1 < gy ? y + 1 : y); b++)
@@ -307,26 +302,45 @@ static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const
               const uint64_t* q = bits + (((size_t)a * gy + b) * gx + c) * 4;
               for (int i = 0; i < 4; i++) w[i] |= q[i];
             }
-        uint64_t* d = dil + (((size_t)z * gy + y) * gx + x) * 5;
-        memcpy(d, w, sizeof(w));
-        d[4] = ((size_t)z * gy + y) * gx + x;
+        uint64_t h = (w[0] * 0x9E3779B97F4A7C15ull) ^ (w[1] * 0xC2B2AE3D27D4EB4Full) ^
+                     (w[2] * 0x165667B19E3779F9ull) ^ (w[3] * 0xD6E8FEB86659FD93ull);
+        h ^= h >> 29;
+        size_t e = (size_t)h & (cap - 1);
+        while (table[e] >= 0 && memcmp(uniq + (size_t)table[e] * 4, w, sizeof(w)) != 0)
+          e = (e + 1) & (cap - 1);
+        if (table[e] < 0) {
+          if (nsets == ucap) {
+            ucap *= 2;
+            uint64_t* u2 = (uint64_t*)realloc(uniq, ucap * 4 * sizeof(uint64_t));
+            mc_class_curve* c2 = (mc_class_curve*)realloc(cur, sizeof(mc_class_curve) * ucap);
+            if (u2) uniq = u2;
+            if (c2) cur = c2;
+            if (!u2 || !c2) {
+              oom = 1;
+              break;
+            }
+          }
+          memcpy(uniq + nsets * 4, w, sizeof(w));
+          mc_class_curve* c = &cur[nsets];
+          for (int k = 0; k < MC_NBINS; k++) c->curve[k] = 0.0f;
+          for (int l = 0; l < MC_MAX_LABELS; l++)
+            if (w[l >> 6] >> (l & 63) & 1)
+              for (int k = 0; k < MC_NBINS; k++)
+                if (L->mu[l][k] > c->curve[k]) c->curve[k] = L->mu[l][k];
+          c->id = (int)nsets;
+          table[e] = (int32_t)nsets++;
+        }
+        set_class[((size_t)z * gy + y) * gx + x] = table[e];  /* per cell: its set, for now */
       }
-  /* distinct label sets, each with its curve */
-  qsort(dil, nc, 5 * sizeof(uint64_t), mc_cmp_bits4);
-  size_t nsets = 0;
-  for (size_t i = 0; i < nc; i++) {
-    const uint64_t* d = dil + i * 5;
-    if (i == 0 || memcmp(d, dil + (i - 1) * 5, 4 * sizeof(uint64_t)) != 0) {
-      mc_class_curve* c = &cur[nsets];
-      for (int k = 0; k < MC_NBINS; k++) c->curve[k] = 0.0f;
-      for (int l = 0; l < MC_MAX_LABELS; l++)
-        if (d[l >> 6] >> (l & 63) & 1)
-          for (int k = 0; k < MC_NBINS; k++)
-            if (L->mu[l][k] > c->curve[k]) c->curve[k] = L->mu[l][k];
-      c->id = (int)nsets;
-      nsets++;
-    }
-    set_class[d[4]] = (int)nsets - 1;  /* per cell: its set, for now */
+  free(table);
+  free(uniq);
+  if (oom) {
+    free(cur);
+    free(set_class);
+    free(set_to_class);
+    free(remap);
+    free(pre);
+    return MONTE_ENOMEM;
   }
   /* sets with equal curves -> one class */
   qsort(cur, nsets, sizeof(mc_class_curve), mc_cmp_curve);
@@ -345,7 +359,6 @@ static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const
     qsort(cur, ncls, sizeof(mc_class_curve), mc_cmp_curve_level);
     mc_class_curve* merged = (mc_class_curve*)malloc(sizeof(mc_class_curve) * MC_MAX_CLASSES);
     if (!merged) {
-      free(dil);
       free(cur);
       free(set_class);
       free(set_to_class);
@@ -374,19 +387,31 @@ static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const
       L->maj[c][k].inv = m > 0.0f ? 1.0f / m : 3.0e38f;
     }
   for (size_t i = 0; i < nc; i++) cls[i] = (uint16_t)remap[set_to_class[set_class[i]]];
-  /* leg lengths, class by class: pre = prefix sums over the grid of "the
-   * cell holds a label above the class's curve" */
+  /* leg lengths: pre = prefix sums over the grid of "the cell holds a
+   * label above the class's curve", one grid per distinct set of such
+   * labels (classes that share it share the grid) */
+  uint64_t bad[MC_MAX_CLASSES][4];
+  int present[MC_MAX_CLASSES];
   for (int c = 0; c < ncls; c++) {
-    uint64_t bad[4] = {0, 0, 0, 0};
+    present[c] = 0;
+    for (int i = 0; i < 4; i++) bad[c][i] = 0;
     for (int l = 0; l < MC_MAX_LABELS; l++)
       for (int k = 0; k < MC_NBINS; k++)
         if (L->mu[l][k] > cur[c].curve[k]) {
-          bad[l >> 6] |= 1ull << (l & 63);
+          bad[c][l >> 6] |= 1ull << (l & 63);
           break;
         }
-    int any = 0;
-    for (size_t i = 0; i < nc; i++) any |= (cls[i] & 0xff) == c;
-    if (!any) continue;
+  }
+  for (size_t i = 0; i < nc; i++) present[cls[i] & 0xff] = 1;
+  for (int c = 0; c < ncls; c++) {
+    if (!present[c]) continue;
+    uint64_t group = 0;  /* present classes with c's set, c first */
+    for (int c2 = c; c2 < ncls; c2++)
+      if (present[c2] && memcmp(bad[c2], bad[c], sizeof(bad[c])) == 0) {
+        group |= 1ull << c2;
+        if (c2 != c) present[c2] = 0;
+      }
+    const uint64_t* bd = bad[c];
 #define MC_PRE(x, y, z) pre[((size_t)(z) * (gy + 1) + (size_t)(y)) * (gx + 1) + (size_t)(x)]
     for (int z = 0; z <= gz; z++)
       for (int y = 0; y <= gy; y++)
@@ -396,7 +421,7 @@ static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const
             continue;
           }
           const uint64_t* q = bits + (((size_t)(z - 1) * gy + (y - 1)) * gx + (x - 1)) * 4;
-          const int32_t v = ((q[0] & bad[0]) | (q[1] & bad[1]) | (q[2] & bad[2]) | (q[3] & bad[3])) != 0;
+          const int32_t v = ((q[0] & bd[0]) | (q[1] & bd[1]) | (q[2] & bd[2]) | (q[3] & bd[3])) != 0;
           MC_PRE(x, y, z) = v + MC_PRE(x - 1, y, z) + MC_PRE(x, y - 1, z) + MC_PRE(x, y, z - 1) -
                             MC_PRE(x - 1, y - 1, z) - MC_PRE(x - 1, y, z - 1) -
                             MC_PRE(x, y - 1, z - 1) + MC_PRE(x - 1, y - 1, z - 1);
@@ -405,26 +430,27 @@ static inline int mc_macro_classes(const mc_params* P, mc_local_tables* L, const
       for (int y = 0; y < gy; y++)
         for (int x = 0; x < gx; x++) {
           const size_t i = ((size_t)z * gy + y) * gx + x;
-          if ((cls[i] & 0xff) != c) continue;
-          int r = 1;
-          while (r < MC_MAX_LEG_CELLS) {
-            const int q = r + 1;
+          const int ci = cls[i] & 0xff;
+          if (!(group >> ci & 1)) continue;
+          /* the box of radius 1 is clean by construction and cleanness only
+           * shrinks with the radius: bisect for the largest clean one */
+          int r = 1, hi = MC_MAX_LEG_CELLS;
+          while (r < hi) {
+            const int q = (r + hi + 1) >> 1;
             const int x0 = x - q > 0 ? x - q : 0, x1 = x + q + 1 < gx ? x + q + 1 : gx;
             const int y0 = y - q > 0 ? y - q : 0, y1 = y + q + 1 < gy ? y + q + 1 : gy;
             const int z0 = z - q > 0 ? z - q : 0, z1 = z + q + 1 < gz ? z + q + 1 : gz;
             const int32_t n = MC_PRE(x1, y1, z1) - MC_PRE(x0, y1, z1) - MC_PRE(x1, y0, z1) -
                               MC_PRE(x1, y1, z0) + MC_PRE(x0, y0, z1) + MC_PRE(x0, y1, z0) +
                               MC_PRE(x1, y0, z0) - MC_PRE(x0, y0, z0);
-            if (n) break;
-            r = q;
+            if (n) hi = q - 1; else r = q;
           }
-          cls[i] = (uint16_t)(c | (r << 8));
+          cls[i] = (uint16_t)(ci | (r << 8));
         }
 #undef MC_PRE
   }
   free(remap);
   free(set_to_class);
-  free(dil);
   free(cur);
   free(set_class);
   free(pre);
