@@ -253,8 +253,8 @@ def mc_cpu_baseline(g, inp, per=256):
 # at 16 histories per pixel per transport (`bench.py --mc-case` under ncu
 # with smsp__inst_executed.sum and smsp__thread_inst_executed.sum: 3,145,728
 # histories per launch), for the issue roofline of the Monte Carlo line.
-MC_PROFILE = {"global": {"warp_inst_per_history": 520.0, "lanes_per_instruction": 17.90},
-              "local": {"warp_inst_per_history": 240.9, "lanes_per_instruction": 12.40}}
+MC_PROFILE = {"global": {"warp_inst_per_history": 518.0, "lanes_per_instruction": 17.97},
+              "local": {"warp_inst_per_history": 240.5, "lanes_per_instruction": 12.42}}
 
 
 def mc_bench(ctx, device, steps=3, per=509, with_cpu=True):

@@ -405,7 +405,10 @@ int monte_mc_sample_energies(monte_ctx* ctx, const monte_spectrum* spec, uint64_
 
 /* Run the Monte Carlo.  primary and scatter are int64 [n_views][nu][nv]
  * tallies that the call ADDS to (zero them first); they follow `mem`.
- * stats may be NULL.  Replaces the projection launch of
+ * With MONTE_MEM_DEVICE the labels and both tallies must be memory the GPU
+ * addresses directly (device, managed, or pinned host memory mapped at the
+ * same address); anything else is rejected with MONTE_EINVAL before any
+ * work.  stats may be NULL.  Replaces the projection launch of
  * monte_cu/CBCT_real325im.cu:235-248. */
 int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom* ph,
                  const monte_xcom* xcom, const monte_spectrum* spec, const monte_mc_request* run,

@@ -148,6 +148,21 @@ int monte_xcom_parse_csv(const char* text, size_t len, float* coherent, float* i
   return MONTE_OK;
 }
 
+namespace {
+// Whether the GPU can address p directly: device or managed memory, or
+// pinned host memory mapped at the same address.  Pageable host memory
+// (cudaMemoryTypeUnregistered) would fault the kernel.
+bool gpu_addressable(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged ||
+         (a.type == cudaMemoryTypeHost && a.devicePointer == p);
+}
+}  // namespace
+
 int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom* ph,
                  const monte_xcom* xcom, const monte_spectrum* spec, const monte_mc_request* run,
                  int64_t* primary, int64_t* scatter, monte_mc_stats* stats, int mem) {
@@ -155,6 +170,10 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
   if (!g || !ph || !xcom || !spec || !run || !primary || !scatter || !ph->labels)
     return set_error(ctx, MONTE_EINVAL, "null argument");
   MONTE_TRY(check_mem(ctx, mem));
+  if (mem == MONTE_MEM_DEVICE &&
+      !(gpu_addressable(ph->labels) && gpu_addressable(primary) && gpu_addressable(scatter)))
+    return set_error(ctx, MONTE_EINVAL,
+                     "MONTE_MEM_DEVICE: labels, primary and scatter must be device memory");
   mc_params P;
   const char* why = "";
   if (mc_setup_params(g, ph, run, &P, &why) != MONTE_OK) return set_error(ctx, MONTE_EINVAL, "%s", why);

@@ -108,6 +108,31 @@ def test_noisy_maps_against_fp64_oracle(ctx, variant):
     assert err < 1e-5, (variant, err)
 
 
+@pytest.mark.parametrize("variant", [33, 34, 35, 36, 38, 39])
+def test_noisy_maps_wide_anchor_shapes(ctx, variant):
+    """The same check for the shapes that anchor every 20 to 32 voxels,
+    which need the rows to advance slowly along z: the benchmark's
+    magnification (SOD 500,
+    SDD 1000 mm, 0.8 mm pixels, 0.4 mm voxels; ~1.1 rows per voxel) on a
+    129^3 volume, 90 views of 256 x 192, 30 histories per pixel."""
+    from inputs import noisy_counts_map
+    g = abi.fdk_geom_recon325(n_views=90, nu=256, nv=192, pitch_mm=0.8, n=129, voxel_mm=0.4)
+    proj = noisy_counts_map(g.n_views, g.nu, g.nv, 30, 129)
+    f64 = oracle.fdk_filter(g, proj, precise=True)
+    v64 = oracle.fdk_backproject(g, f64)
+    p = torch.from_numpy(proj).cuda()
+    xy = torch.empty((g.nz, g.ny, g.nx), device="cuda")
+    try:
+        ctx.set_bp_variant(variant)
+        ctx.fdk(g, p, xy, filter_mode=abi.MONTE_FILTER_FP32, bp_mode=abi.MONTE_BP_TILED)
+        ctx.check_status()
+        assert ctx.last_bp_variant() == variant
+    finally:
+        ctx.set_bp_variant(-1)
+    err = rel_rms(xy.cpu().numpy(), v64)
+    assert err < 1e-5, (variant, err)
+
+
 def test_host_memory_path_equals_device_path(ctx):
     g = abi.fdk_geom_reference65()
     proj = fdk_projections(360, 65, 65, 11)

@@ -147,6 +147,17 @@ def test_bad_arguments(ctx):
     g.sdd = 10.0  # detector inside the source distance
     with pytest.raises(MonteError):
         ctx.mc_run(g, dev, abi.mc_request(1, 1, (0, 1), (0, 64), (0, 64)), prim, prim.clone())
+    # MONTE_MEM_DEVICE with a pageable host tally: rejected before any work
+    # (the kernel would fault on it)
+    import ctypes as C
+    g = cfg1_geom()
+    host = np.zeros((g.n_views, g.nu, g.nv), np.int64)
+    st = abi.McStats()
+    rc = ctx.lib.monte_mc_run(ctx.h, C.byref(g), C.byref(dev.phantom), C.byref(dev.xcom),
+                              C.byref(dev.spectrum), C.byref(abi.mc_request(1, 1, (0, 1), (0, 64), (0, 64))),
+                              host.ctypes.data, prim.data_ptr(), C.byref(st), abi.MONTE_MEM_DEVICE)
+    assert rc == abi.MONTE_EINVAL
+    assert int(prim.abs().sum()) == 0
 
 
 def test_fan_beam_one_row_detector_replay(ctx):
