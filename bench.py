@@ -58,9 +58,13 @@ def parse():
 
 
 WORKLOAD = "fdk: 360 views x 512(u) x 384(v) FP32 @0.8mm, SOD 500, SDD 1000 mm -> 325^3 FP32 @0.4mm"
-# measured DRAM traffic per backprojection launch of WORKLOAD, by tile shape
-BP_TRAFFIC = {33: 280.64e6 + 127.57e6, 29: 280.82e6 + 127.04e6, 24: 342.49e6 + 144.32e6, 26: 980.36e6 + 178.60e6,
-              16: 904.65e6 + 164.43e6}
+# DRAM traffic per backprojection launch of WORKLOAD, by tile shape:
+# dram__bytes_read.sum + dram__bytes_write.sum from one-pass ncu captures of
+# `bench.py --no-mc --no-plain --no-cpu-baseline --no-batch --no-diff
+# --tile T --steps 3 --warmup 3` (shape 36 captured with the folded-weight
+# voxel loop; the others with the earlier loop, which moves the same bytes)
+BP_TRAFFIC = {36: 306.77e6 + 125.24e6, 33: 280.64e6 + 127.57e6, 29: 280.82e6 + 127.04e6,
+              24: 342.49e6 + 144.32e6, 26: 980.36e6 + 178.60e6, 16: 904.65e6 + 164.43e6}
 
 
 def geometry(small=False):

@@ -352,9 +352,7 @@ int create_plan(monte_ctx* ctx, const monte_xcom* xcom, const monte_batch_job* j
         tuned.push_back({key, v});
       }
     } else {
-      v = ctx->bp_tune_choice;
-      if (v < 0 || !fdk_bp_tiled_supported(b.fdk, v)) v = 0;
-      if (!fdk_bp_tiled_supported(b.fdk, v)) v = -1;
+      v = fdk_bp_pick(b.fdk, ctx->bp_tune_choice);
     }
     b.bp_variant = v;
   }

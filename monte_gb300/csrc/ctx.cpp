@@ -133,6 +133,7 @@ int monte_ctx_destroy(monte_ctx* ctx) {
   monte::release(ctx->mc_tables);
   monte::release(ctx->mc_views);
   monte::release(ctx->mc_mclass);
+  monte::release(ctx->mc_label_copy);
   monte::release(ctx->mc_pixels);
   if (ctx->d_status) cudaFree(ctx->d_status);
   for (cudaEvent_t ev : ctx->pipe_ev)

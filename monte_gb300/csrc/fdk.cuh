@@ -166,6 +166,11 @@ int fdk_bp_tiled_variants();
 // padded: the caller provides the padded copy of the filtered projections
 // (needed by the per-warp shapes when nu is not a multiple of 4)
 bool fdk_bp_tiled_supported(const FdkDev& d, int variant, bool padded = false);
+// The tile shape to run: `want` when it fits the geometry, else the first
+// of a fixed list of robust shapes that does (the one-warp shapes with 48
+// and 32 voxels per lane, then two-warp and shared-ring ones), else -1
+// (the plain backprojector).  want < 0: no choice made (not autotuned).
+int fdk_bp_pick(const FdkDev& d, int want, bool padded = false);
 
 #ifdef __CUDACC__
 // Shared by the plain and tiled kernels: bilinear read of filtered[view]

@@ -317,9 +317,8 @@ int run_bp(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_filtered, flo
       if (ep != cudaSuccess) return cuda_fail(ctx, ep, "row padding launch");
     }
     const bool pad = padded != nullptr;
-    int variant = ctx->bp_tune_choice;
-    if (variant < 0 || !fdk_bp_tiled_supported(d, variant, pad)) variant = 0;
-    if (!fdk_bp_tiled_supported(d, variant, pad)) {
+    const int variant = fdk_bp_pick(d, ctx->bp_tune_choice, pad);
+    if (variant < 0) {
       // the footprint of a voxel block does not fit a shared-memory box:
       // the one-voxel-per-thread kernel handles any geometry
       e = launch_fdk_bp_plain(d, views, viewsd, d_filtered, d_xy, d_zy, ctx->stream);
@@ -506,9 +505,8 @@ int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, int stages, cons
     if (bp_mode != MONTE_BP_TILED || g->s_begin != 0 || g->s_end != g->nx) return 0;
     const FdkDev d = make_fdk_dev(*g);
     const bool pad = g->nu % 4 != 0;  // tiles from a padded copy
-    variant = ctx->bp_tune_choice;
-    if (variant < 0 || !fdk_bp_tiled_supported(d, variant, pad)) variant = 0;
-    if (!fdk_bp_tiled_supported(d, variant, pad)) return 0;
+    variant = fdk_bp_pick(d, ctx->bp_tune_choice, pad);
+    if (variant < 0) return 0;
     mxy = (float*)host_mapped(vol_xy);
     mzy = vol_zy ? (float*)host_mapped(vol_zy) : nullptr;
     if (!mxy || (vol_zy && !mzy)) return 0;

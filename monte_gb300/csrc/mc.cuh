@@ -44,6 +44,10 @@ inline void mc_stats_from(const unsigned long long* h, monte_mc_stats* s) {
 }
 
 cudaError_t launch_mc(const McDev& d, int kernel, int sm_count, cudaStream_t st);
+// *diff = 1 if the n bytes at a and b differ anywhere (*diff is not
+// cleared first).
+cudaError_t launch_bytes_differ(const uint8_t* a, const uint8_t* b, size_t n, int* diff,
+                                int sm_count, cudaStream_t st);
 
 // Jobs one batched persistent launch can carry.
 constexpr int kMaxBatchJobs = 1024;

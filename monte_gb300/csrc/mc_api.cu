@@ -33,6 +33,30 @@ int mc_build_macro(monte_ctx* ctx, const monte_mc_phantom* ph, const monte_xcom*
                    std::vector<uint16_t>* cls, std::vector<uint8_t>* key) {
   mc_setup_local(ph, x, L);
   const size_t cells = (size_t)P.mgx * P.mgy * P.mgz;
+  const size_t nlab = (size_t)ph->nx * ph->ny * ph->nz;
+  if (key) {
+    // the class grid depends on the grid, mu per label and the labels
+    const int dims[7] = {P.mgx, P.mgy, P.mgz, P.mshift, ph->nx, ph->ny, ph->nz};
+    key->resize(sizeof(dims) + sizeof(L->mu));
+    memcpy(key->data(), dims, sizeof(dims));
+    memcpy(key->data() + sizeof(dims), L->mu, sizeof(L->mu));
+    if (labels_on_device && *key == ctx->mc_macro_key && ctx->mc_label_bytes == nlab) {
+      // same grid and attenuation: the tables hold if the labels are those
+      // they were built from, which the device checks against its copy (a
+      // 4-byte answer, where the label sets would be 32 bytes per cell)
+      MONTE_TRY(ensure_slot(ctx, kScratchAux2, sizeof(int), "label comparison flag"));
+      int* dflag = (int*)ctx->scratch[kScratchAux2].ptr;
+      MONTE_CUDA(ctx, cudaMemsetAsync(dflag, 0, sizeof(int), ctx->stream));
+      cudaError_t e = launch_bytes_differ(ph->labels, (const uint8_t*)ctx->mc_label_copy.ptr, nlab,
+                                          dflag, ctx->sm_count, ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "label comparison");
+      int differ = 1;
+      MONTE_CUDA(ctx, cudaMemcpyAsync(&differ, dflag, sizeof(int), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+      MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!differ) return MONTE_OK;  // cls left empty: reuse the device copy
+    }
+  }
   std::vector<uint64_t> bits(cells * 4);
   if (labels_on_device) {
     MONTE_TRY(ensure_slot(ctx, kScratchAux3, cells * 4 * sizeof(uint64_t), "macro-cell label sets"));
@@ -44,16 +68,13 @@ int mc_build_macro(monte_ctx* ctx, const monte_mc_phantom* ph, const monte_xcom*
     MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   } else {
     mc_macro_bits_host(ph, ph->labels, &P, bits.data());
-  }
-  if (key) {
-    // the class grid depends on the grid, mu per label and the label sets
-    const int dims[4] = {P.mgx, P.mgy, P.mgz, P.mshift};
-    key->resize(sizeof(dims) + sizeof(L->mu) + bits.size() * sizeof(uint64_t));
-    uint8_t* k = key->data();
-    memcpy(k, dims, sizeof(dims));
-    memcpy(k + sizeof(dims), L->mu, sizeof(L->mu));
-    memcpy(k + sizeof(dims) + sizeof(L->mu), bits.data(), bits.size() * sizeof(uint64_t));
-    if (*key == ctx->mc_macro_key) return MONTE_OK;  // cls left empty: reuse the device copy
+    if (key) {
+      // host labels: the cells' label sets complete the key
+      const size_t k0 = key->size();
+      key->resize(k0 + bits.size() * sizeof(uint64_t));
+      memcpy(key->data() + k0, bits.data(), bits.size() * sizeof(uint64_t));
+      if (*key == ctx->mc_macro_key) return MONTE_OK;  // cls left empty: reuse
+    }
   }
   cls->assign(cells, 0);
   if (mc_macro_classes(&P, L, bits.data(), cls->data()) != MONTE_OK)
@@ -213,6 +234,14 @@ int monte_mc_run(monte_ctx* ctx, const monte_mc_geom* g, const monte_mc_phantom*
       MONTE_CUDA(ctx, cudaMemcpyAsync((char*)ctx->mc_mclass.ptr + sizeof(mc_local_tables),
                                       cls.data(), cls.size() * 2, cudaMemcpyHostToDevice,
                                       ctx->stream));
+      ctx->mc_label_bytes = 0;
+      if (mem == MONTE_MEM_DEVICE) {
+        // the labels these tables were built from, for the next call's check
+        MONTE_TRY(ensure(ctx, ctx->mc_label_copy, nlab, "label copy"));
+        MONTE_CUDA(ctx, cudaMemcpyAsync(ctx->mc_label_copy.ptr, ph->labels, nlab,
+                                        cudaMemcpyDefault, ctx->stream));
+        ctx->mc_label_bytes = nlab;
+      }
       ctx->mc_macro_key.swap(key);
     }
   }

@@ -452,6 +452,38 @@ cudaError_t launch_mc_macro_bits(const uint8_t* labels, const mc_params& P, unsi
   return cudaGetLastError();
 }
 
+namespace {
+__global__ void bytes_differ_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b,
+                                    size_t n, bool vec, int* __restrict__ diff) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool ne = false;
+  size_t done = 0;
+  if (vec) {  // both 16-byte aligned: 16 bytes per load
+    const uint4* a4 = reinterpret_cast<const uint4*>(a);
+    const uint4* b4 = reinterpret_cast<const uint4*>(b);
+    const size_t n4 = n / 16;
+    for (size_t i = i0; i < n4; i += stride) {
+      const uint4 x = a4[i], y = b4[i];
+      ne |= (x.x != y.x) | (x.y != y.y) | (x.z != y.z) | (x.w != y.w);
+    }
+    done = n4 * 16;
+  }
+  for (size_t i = done + i0; i < n; i += stride) ne |= a[i] != b[i];
+  if (__any_sync(__activemask(), ne) && ne) *diff = 1;
+}
+}  // namespace
+
+cudaError_t launch_bytes_differ(const uint8_t* a, const uint8_t* b, size_t n, int* diff,
+                                int sm_count, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
+  const size_t want = (n / (vec ? 16 : 1) + 255) / 256;
+  const unsigned blocks = (unsigned)(want < 8ull * sm_count ? (want ? want : 1) : 8ull * sm_count);
+  bytes_differ_kernel<<<blocks, 256, 0, st>>>(a, b, n, vec, diff);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mc_energies(const mc_tables* T, uint64_t seed, const monte_philox_keys& keys,
                                uint32_t job, unsigned long long n, float* out, int sm_count,
                                cudaStream_t st) {

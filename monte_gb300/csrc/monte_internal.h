@@ -41,10 +41,13 @@ struct monte_ctx {
   // cached MC device tables
   std::vector<uint8_t> mc_key;
   // what the local-majorant tables in mc_mclass were built from (phantom
-  // grid, label materials and densities, attenuation tables, the cells'
-  // label sets): a call with the same key reuses them
+  // grid, label materials and densities, attenuation tables, and for host
+  // labels the cells' label sets): a call with the same key reuses them.
+  // For device labels the label volume itself is kept in mc_label_copy
+  // (mc_label_bytes of it) and compared on the device.
   std::vector<uint8_t> mc_macro_key;
-  monte::DevBuf mc_tables, mc_views, mc_pixels, mc_mclass;
+  monte::DevBuf mc_tables, mc_views, mc_pixels, mc_mclass, mc_label_copy;
+  size_t mc_label_bytes = 0;
   // device-side error flag word for bounded waits / kernel status
   int* d_status = nullptr;
   // autotuned backprojection tile choice, keyed by geometry

@@ -72,6 +72,32 @@ def test_replay_is_bit_exact(ctx, spectrum, flags):
         assert (st["majorant_legs"] > 0) == bool(flags & abi.MONTE_MC_LOCAL_MAJORANT)
 
 
+def test_local_majorant_tables_follow_the_labels(ctx):
+    """The context keeps the local-majorant tables of its last phantom and
+    reuses them while the labels are the same bytes (checked on the device
+    against its copy).  Labels changed in place between two calls on the
+    same buffer must rebuild them: the second run equals the CPU replay of
+    the changed phantom, and the label check then reuses the new tables."""
+    g = cfg1_geom(abi.MONTE_MC_STALE_SIN_PHI | abi.MONTE_MC_LOCAL_MAJORANT)
+    dev = cfg1_inputs("cuda")
+    req = abi.mc_request(4242, 4, (3, 5), (0, 64), (0, 64))
+    _gpu_run(ctx, g, dev, req)  # builds and keeps the tables
+    host = cfg1_inputs(None)
+    lab = host.labels.copy()
+    # turn a slab of the cylinder into the densest insert's label: a
+    # material the old tables' majorants around it do not cover
+    dense = int(lab.max())
+    slab = lab[20:45, 10:30, 25:40]
+    lab[20:45, 10:30, 25:40] = np.where(slab > 0, dense, slab)
+    dev.labels.copy_(torch.from_numpy(lab).to(dev.labels.device))
+    host.labels[...] = lab  # the same array the phantom struct points at
+    p_ref, s_ref, st_ref = oracle.mc_run(g, host, req)
+    for _ in range(2):  # rebuilt, then reused
+        p, s, st = _gpu_run(ctx, g, dev, req)
+        assert np.array_equal(p, p_ref) and np.array_equal(s, s_ref)
+        assert st["majorant_legs"] == st_ref["majorant_legs"]
+
+
 def test_split_runs_sum_to_the_whole(ctx):
     """Any partition of (views, pixels) reproduces the single run's tallies:
     the sharding contract for multi-GPU runs."""
