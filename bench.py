@@ -181,11 +181,13 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
-def cpu_baseline(g, budget_s=20.0):
+def cpu_baseline(g, slices_per_core=8):
     """Time the CPU oracle (FP64 restatement of recon/bp3d20.cpp, all host
     threads) on a bounded sample and scale to GUPS for the full workload:
-    the filter on a few views and the backprojection on a few z-slices of
-    all views; T = n_views * t_view + updates * t_update."""
+    the filter on a few views and the backprojection on slices_per_core
+    z-slices per host thread of all views (8: ~10 s on 16 cores; the
+    reference arm, which repeats it every step, takes 1);
+    T = n_views * t_view + updates * t_update."""
     import oracle
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
@@ -199,7 +201,7 @@ def cpu_baseline(g, budget_s=20.0):
     t_view = (time.perf_counter() - t0) / nviews_s
     filt = np.zeros((g.n_views, g.nv, g.nu), np.float32)
     filt[:] = rng.random((g.nv, g.nu), dtype=np.float32)
-    nz_s = max(2, min(cores, 16))
+    nz_s = max(2, min(g.nz, slices_per_core * min(cores, 16)))
     t0 = time.perf_counter()
     oracle.fdk_backproject(g, filt, z_range=(g.nz // 2, g.nz // 2 + nz_s))
     t_bp = time.perf_counter() - t0
@@ -233,11 +235,12 @@ def mc_workload():
     return g, lab, make
 
 
-def mc_cpu_baseline(g, inp, per=256):
+def mc_cpu_baseline(g, inp, per=32768):
     """The CPU replay harness (oracle/mc_oracle.c: the reference kernel's
     history loop restated, the same step functions and streams, all host
-    cores) on a bounded sample of the 325^3 workload: view 0, the central
-    64 x 64 pixels, `per` histories each (1.05e6 histories)."""
+    cores, the reference's single majorant) on a bounded sample of the
+    325^3 workload: view 0, the central 64 x 64 pixels, `per` histories
+    each (1.34e8 histories, ~11 s on 16 cores)."""
     import oracle
     from monte_gb300 import abi
     cores = os.cpu_count() or 1
@@ -481,7 +484,7 @@ def run_reference(args):
     vals = []
     cb = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(g)
+        cb = cpu_baseline(g, slices_per_core=1)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)
