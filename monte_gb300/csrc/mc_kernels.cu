@@ -204,6 +204,13 @@ __device__ __forceinline__ void persistent_body(const McDev& d) {
       if (mc_flight_event(&d.P, d.T, d.L, d.labels, d.mclass, &p)) st[1]++; else st[9]++;
       if (p.state == MC_DEAD) st[5]++;
     }
+    // ---- real collisions: the type at once (absorption ends the history,
+    // Rayleigh flies on); Compton waits for the batch below ---------------
+    if (p.state == MC_COLLIDED) {
+      const int n0 = p.n_int;
+      p.state = p.n_int >= d.P.max_int ? MC_DEAD : mc_interact_type(&d.P, d.T, &p);
+      count_event(p, n0, st);
+    }
     // ---- escaped photons: warp-aggregated tally --------------------------
     long long key = -1;
     long long cell = -1;
@@ -222,15 +229,11 @@ __device__ __forceinline__ void persistent_body(const McDev& d) {
       }
       if (kind == 0) st[3]++; else st[4]++;  // no run-time index: st stays in registers
     }
-    // ---- real collisions, processed as a batch ---------------------------
-    const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
+    // ---- Compton scatterings, processed as a batch ------------------------
+    const unsigned coll = __ballot_sync(FULL, p.state == MC_COMPTON);
     const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
     if (coll && (__popc(coll) >= CB || fly == 0)) {
-      if (p.state == MC_COLLIDED) {
-        const int n0 = p.n_int;
-        p.state = mc_after_collision(&d.P, d.T, &p);
-        count_event(p, n0, st);
-      }
+      if (p.state == MC_COMPTON) p.state = mc_compton(&d.P, &p);
     }
   }
   st[2] += (unsigned long long)p.n_int;
@@ -317,6 +320,11 @@ __global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
       if (mc_flight_event(&J->P, J->T, J->L, J->labels, J->mclass, &p)) st[1]++; else st[9]++;
       if (p.state == MC_DEAD) st[5]++;
     }
+    if (p.state == MC_COLLIDED) {
+      const int n0 = p.n_int;
+      p.state = p.n_int >= J->P.max_int ? MC_DEAD : mc_interact_type(&J->P, J->T, &p);
+      count_event(p, n0, st);
+    }
     long long cell = -1;
     int kind = 0;
     if (p.state == MC_ESCAPED) {
@@ -334,14 +342,10 @@ __global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
       if (lane == __ffs(grp) - 1) atomicAdd(dst, (unsigned long long)__popc(grp));
       if (kind == 0) st[3]++; else st[4]++;  // no run-time index: st stays in registers
     }
-    const unsigned coll = __ballot_sync(FULL, p.state == MC_COLLIDED);
+    const unsigned coll = __ballot_sync(FULL, p.state == MC_COMPTON);
     const unsigned fly = __ballot_sync(FULL, p.state == MC_FLY);
     if (coll && (__popc(coll) >= kCollideBatch || fly == 0)) {
-      if (p.state == MC_COLLIDED) {
-        const int n0 = p.n_int;
-        p.state = mc_after_collision(&J->P, J->T, &p);
-        count_event(p, n0, st);
-      }
+      if (p.state == MC_COMPTON) p.state = mc_compton(&J->P, &p);
     }
   }
   st[2] += (unsigned long long)p.n_int;

@@ -103,7 +103,7 @@ typedef struct {
   float b, sin_t, cos_t; /* v pixel: zl, sin/cos(pi/2 - atan(zl/sdd)) */
 } mc_pixel;
 
-enum { MC_FLY = 0, MC_COLLIDED = 1, MC_ESCAPED = 2, MC_DEAD = 3 };
+enum { MC_FLY = 0, MC_COLLIDED = 1, MC_ESCAPED = 2, MC_DEAD = 3, MC_COMPTON = 4 };
 enum { MC_EV_NONE = 0, MC_EV_RAYLEIGH = 1, MC_EV_COMPTON = 2, MC_EV_PHOTO = 3 };
 
 typedef struct {
@@ -391,7 +391,13 @@ MONTE_HD long long mc_detector_index(const mc_params* P, const mc_view* V, const
  * the new state: MC_DEAD (photo-absorption or numerical failure) or MC_FLY
  * (Rayleigh: direction kept, :656-671; Compton: Kahn sampling of
  * Klein-Nishina, :701-736, energy 511/lambda', rotation :768-781). */
-MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
+/* The first part of an interaction, its type: MC_DEAD (photoelectric
+ * absorption, or a label without a material), MC_FLY (Rayleigh: the
+ * direction is kept), or MC_COMPTON, for which mc_compton follows.  Split
+ * so that a kernel can settle the short outcomes at once and run the long
+ * Compton sampling for several lanes together; the draws are the same
+ * either way. */
+MONTE_HD int mc_interact_type(const mc_params* P, const mc_tables* T, mc_photon* p) {
   int mat = T->label_material[p->label];
   if (mat < 0) return MC_DEAD;
   float sc = monte_uniform_keys(&p->rng, &P->keys);
@@ -406,6 +412,11 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
     return MC_FLY;
   }
   p->last = MC_EV_COMPTON;
+  return MC_COMPTON;
+}
+
+/* The Compton part of an interaction (after mc_interact_type). */
+MONTE_HD int mc_compton(const mc_params* P, mc_photon* p) {
   /* Kahn's rejection sampling of lambda' = rho * lambda (:701-736) */
   float lambda = 511.0f / p->E;
   float lam2 = lambda + 2.0f;
@@ -467,6 +478,11 @@ MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
   p->n_compton++;
   p->steps = 0;
   return MC_FLY;
+}
+
+MONTE_HD int mc_interact(const mc_params* P, const mc_tables* T, mc_photon* p) {
+  const int s = mc_interact_type(P, T, p);
+  return s == MC_COMPTON ? mc_compton(P, p) : s;
 }
 
 /* Whether an escaped photon is tallied, and into which tally:
