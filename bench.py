@@ -261,8 +261,8 @@ def mc_cpu_baseline(g, inp, per=32768):
 # at 16 histories per pixel per transport (`bench.py --mc-case` under ncu
 # with smsp__inst_executed.sum and smsp__thread_inst_executed.sum: 3,145,728
 # histories per launch), for the issue roofline of the Monte Carlo line.
-MC_PROFILE = {"global": {"warp_inst_per_history": 518.0, "lanes_per_instruction": 17.97},
-              "local": {"warp_inst_per_history": 240.5, "lanes_per_instruction": 12.42}}
+MC_PROFILE = {"global": {"warp_inst_per_history": 520.7, "lanes_per_instruction": 17.95},
+              "local": {"warp_inst_per_history": 240.5, "lanes_per_instruction": 12.52}}
 
 
 def mc_bench(ctx, device, steps=3, per=509, with_cpu=True):
