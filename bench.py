@@ -441,6 +441,9 @@ def diff_bench(ctx, device):
         return e0.elapsed_time(e1) / 1e3 / reps
 
     updates = g.nx * g.ny * g.nz * g.n_views
+    # the tile shape for this geometry (its rows advance 2.4 per voxel, where
+    # the benchmark's shape does not fit), as a caller would tune it
+    bp_tile = ctx.fdk_autotune(g)
     # ||A x - p||^2: A x in filtered-space layout [view][v][u]; p transposed alike
     p_vu = p.transpose(1, 2).contiguous()
 
@@ -471,6 +474,7 @@ def diff_bench(ctx, device):
     rays = mg.n_views * mg.nu * mg.nv
     return {"workload": DIFF_WORKLOAD,
             "forward_projector": {"ms": t_fp * 1e3, "gups": updates / t_fp / 1e9},
+            "bp_tile_variant": bp_tile,
             "grad_x_least_squares": {"ms": t_gx * 1e3, "note": "A x - p, then 2 A^T r (tiled)"},
             "grad_p_fdk": {"ms": t_gp * 1e3, "note": "FDK (BF16x3 + tiled), then FDK^T"},
             "siddon_forward": {"ms": t_sf * 1e3, "rays_per_s": rays / t_sf},
