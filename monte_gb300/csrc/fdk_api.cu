@@ -344,12 +344,15 @@ size_t vol_bytes(const monte_fdk_geom* g) {
 
 // ---- FDK from and to host memory, pipelined -------------------------------
 //
-// The views are cut into ranges that grow fivefold, the first 1/31 of the
-// scan (360 views: 0-12, 12-72, 72-360): on the 325^3 workload a view
-// uploads in 3.7 us (786 KB at 210 GB/s) and backprojects in 23 us, so each
-// range's upload hides under the previous range's backprojection with room
-// for a slower link.  (Sixfold from 1/60, 0-6, 6-42, 42-360, left 0.4 ms of
-// the last upload exposed.)  Range i is uploaded on copy_in, filtered on the context's
+// The views are cut into two ranges, the first 2/15 of the scan (360
+// views: 0-48, 48-360): on the 325^3 workload a view uploads in 3.7 us (786
+// KB at 210 GB/s) and backprojects in 23 us, so the second range's upload
+// (1.2 ms at 210 GB/s, 1.4 ms at 170) hides, or nearly, under the first
+// range's backprojection (1.2 ms), and the first range's upload and filter
+// (0.25 ms) stay exposed.  Measured end to end at 202 GB/s: 9.22 ms, against
+// 9.33 ms with a first range of 1/6 and 9.40 ms with three ranges growing
+// fivefold from 1/31 (0-12, 12-72, 72-360): every extra backprojection
+// launch costs more than a smaller first upload saves.  Range i is uploaded on copy_in, filtered on the context's
 // stream as soon as it has landed, and backprojected into the running
 // per-voxel sums (BpPart; one view behind, as the flat-edge reads of a
 // view's last row reach into the next view); the upload of range i+1 runs under the
@@ -388,15 +391,11 @@ int pipe_init(monte_ctx* ctx) {
 
 // View ranges [r[i], r[i+1]) of the pipeline; returns their number.
 int pipe_ranges(int n_views, int* r) {
-  int nr = 0, b = 0, len = std::max(1, (n_views + 30) / 31);
+  const int first = std::max(1, (2 * n_views + 14) / 15);
+  int nr = 0;
   r[0] = 0;
-  while (b < n_views) {
-    int e = std::min(n_views, b + len);
-    if (nr == kPipeMaxRanges - 1 || n_views - e < len) e = n_views;  // fold a short tail in
-    r[++nr] = e;
-    b = e;
-    len *= 5;
-  }
+  r[++nr] = std::min(n_views, first);
+  if (first < n_views) r[++nr] = n_views;
   return nr;
 }
 
