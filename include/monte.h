@@ -255,14 +255,20 @@ int monte_fbp2(monte_ctx* ctx, const monte_fbp2_geom* g, const float* proj, floa
 #define MONTE_MC_NO_RAYLEIGH_TALLY 0x4 /* photons whose last interaction was Rayleigh
                                           are not tallied (monte_cpp/CBCT_real2.cpp:373-397) */
 /* Transport switch (not a reference behaviour): delta tracking against
- * majorants local to macro cells of the phantom (the largest attenuation
- * among the labels of a cell and its 26 neighbours) instead of the
- * reference's single majorant over the whole phantom
- * (monte_cu/CBCT_real325im.cu:866-868).  Exact in distribution -- the
- * same tallies in expectation -- but the random numbers are used
- * differently, so histories differ from those without the flag.  Far fewer
- * virtual collisions where soft tissue or air neighbours bone.  Not
- * supported by monte_mc_run_noalloc. */
+ * majorants local to macro cells of the phantom -- per cell, the largest
+ * attenuation among the labels of the cell and its 26 neighbours, under
+ * which a photon moves as far as no larger attenuation lies -- instead of
+ * the reference's single majorant over the whole phantom
+ * (monte_cu/CBCT_real325im.cu:866-868).  Exact in distribution -- the same
+ * tallies in expectation -- but the random numbers are used differently,
+ * so histories differ from those without the flag.  Far fewer virtual
+ * collisions where soft tissue or air neighbours bone.  The macro cells are
+ * 2^k voxels on a side, the smallest power of two >= 2 that leaves at most
+ * 96 cells along the longest axis.  A context keeps the tables of its last
+ * phantom and reuses them while the grid, the materials and the labels are
+ * unchanged; with device labels it keeps a copy of the label volume
+ * (nx*ny*nz bytes of device memory) and compares it on the device at each
+ * call.  Not supported by monte_mc_run_noalloc. */
 #define MONTE_MC_LOCAL_MAJORANT    0x8
 
 /* Kernels. */
