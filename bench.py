@@ -182,6 +182,19 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu), else the machine type."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(g, slices_per_core=8):
     """Time the CPU oracle (FP64 restatement of recon/bp3d20.cpp, all host
     threads) on a bounded sample and scale to GUPS for the full workload:
@@ -210,7 +223,8 @@ def cpu_baseline(g, slices_per_core=8):
     t_upd = t_bp / upd_s
     updates = g.nx * g.ny * g.nz * g.n_views
     T = g.n_views * t_view + updates * t_upd
-    return {"value": updates / T / 1e9, "unit": "GUPS", "cores": cores, "kind": "port",
+    return {"value": updates / T / 1e9, "unit": "GUPS", "cores": cores, "cpu": cpu_model(),
+            "kind": "port",
             "sample": "oracle filter on %d views + backprojection of %d z-slices x %d views, "
                       "scaled to the full workload (est. %.1f s per FDK)" % (nviews_s, nz_s,
                                                                             g.n_views, T)}
@@ -251,7 +265,7 @@ def mc_cpu_baseline(g, inp, per=32768):
     t0 = time.perf_counter()
     _, _, st = oracle.mc_run(g, inp, req)
     dt = time.perf_counter() - t0
-    return {"value": st["histories"] / dt, "unit": "histories/s", "cores": cores, "kind": "port",
+    return {"value": st["histories"] / dt, "unit": "histories/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
             "sample": "CPU replay of view 0, central 64x64 pixels, %d histories each "
                       "(%d histories, %.1f s)" % (per, st["histories"], dt)}
 
