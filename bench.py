@@ -668,6 +668,15 @@ def run_ours(args):
         "roofline_hbm": {"kernel": "backprojection", "bound": "hbm",
                          "achieved": bp_bytes / t_bp / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": bp_bytes / t_bp / 1e9 / hbm_peak, "traffic": traffic},
+        # the pipe the voxel loop saturates first: its four bilinear taps per
+        # update come from the shared-memory tile, one warp-wide 4-byte load
+        # each, and shared memory delivers 128 bytes per cycle per SM
+        "roofline_smem": {"kernel": "backprojection", "bound": "shared-memory loads",
+                          "achieved": 16.0 * updates / t_bp / 1e9,
+                          "peak": n_sm * 128 * sm_max * 1e6 / 1e9, "unit": "GB/s",
+                          "frac": 16.0 * updates / t_bp / (n_sm * 128 * sm_max * 1e6),
+                          "algorithmic": "4 FP32 taps (16 B) per voxel-view update",
+                          "peak_source": "%d SMs x 128 B x %.0f MHz" % (n_sm, sm_max)},
         "e2e": {"value": e2e_val, "unit": "GUPS",
                 "h2d_bytes_per_step": int(g.n_views * g.nu * g.nv * 4),
                 "d2h_bytes_per_step": int(g.nx * g.ny * g.nz * 4),
