@@ -124,6 +124,7 @@ int monte_ctx_destroy(monte_ctx* ctx) {
   if (ctx->stream && ctx->stream != ctx->own_stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in);
   if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out);
+  if (ctx->filter_stream) cudaStreamSynchronize(ctx->filter_stream);
   for (auto& b : ctx->scratch) monte::release(b);
   monte::release(ctx->fdk_views);
   monte::release(ctx->fdk_viewsd);
@@ -140,6 +141,7 @@ int monte_ctx_destroy(monte_ctx* ctx) {
     if (ev) cudaEventDestroy(ev);
   if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
   if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
+  if (ctx->filter_stream) cudaStreamDestroy(ctx->filter_stream);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return MONTE_OK;

@@ -270,12 +270,13 @@ int prepare_tables(monte_ctx* ctx, const monte_fdk_geom* g) {
 }
 
 int run_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_proj, float* d_filtered,
-               int filter_mode) {
+               int filter_mode, cudaStream_t st = nullptr) {
+  if (!st) st = ctx->stream;
   FdkDev d = make_fdk_dev(*g);
   cudaError_t e;
   if (filter_mode == MONTE_FILTER_FP32) {
     e = launch_fdk_filter_fp32(d, d_proj, (const float*)ctx->fdk_weights.ptr,
-                               (const float*)ctx->fdk_taps.ptr, d_filtered, ctx->stream);
+                               (const float*)ctx->fdk_taps.ptr, d_filtered, st);
   } else if (filter_mode == MONTE_FILTER_BF16X3) {
     if (!bf16x3_supported(d))
       return set_error(ctx, MONTE_EUNSUPPORTED,
@@ -283,7 +284,7 @@ int run_filter(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_proj, flo
                        g->nv);
     e = launch_fdk_filter_bf16x3(d, d_proj, (const float*)ctx->fdk_weights.ptr,
                                  (const uint16_t*)ctx->fdk_bsplit.ptr, d_filtered, ctx->d_status,
-                                 ctx->sm_count, ctx->stream);
+                                 ctx->sm_count, st);
   } else {
     return set_error(ctx, MONTE_EINVAL, "unknown filter mode %d", filter_mode);
   }
@@ -352,10 +353,13 @@ size_t vol_bytes(const monte_fdk_geom* g) {
 // (0.25 ms) stay exposed.  Measured end to end at 202 GB/s: 9.22 ms, against
 // 9.33 ms with a first range of 1/6 and 9.40 ms with three ranges growing
 // fivefold from 1/31 (0-12, 12-72, 72-360): every extra backprojection
-// launch costs more than a smaller first upload saves.  Range i is uploaded on copy_in, filtered on the context's
-// stream as soon as it has landed, and backprojected into the running
-// per-voxel sums (BpPart; one view behind, as the flat-edge reads of a
-// view's last row reach into the next view); the upload of range i+1 runs under the
+// launch costs more than a smaller first upload saves.  Range i is
+// uploaded on copy_in, filtered as soon as it has landed on filter_stream
+// (the greatest priority, so that its blocks take the SMs the previous
+// range's backprojection frees, alongside that launch's last waves), and
+// backprojected on the context's stream into the running per-voxel sums
+// (BpPart; one view behind, as the flat-edge reads of a view's last row
+// reach into the next view); the upload of range i+1 runs under the
 // backprojection of range i, so of the upload only the first, small range
 // stays on the critical path.  The last range's backprojection stores its
 // sums straight into the caller's pinned volume, which spreads the download
@@ -383,6 +387,15 @@ int pipe_init(monte_ctx* ctx) {
     MONTE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
   if (!ctx->copy_out)
     MONTE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+  if (!ctx->filter_stream) {
+    // the greatest priority: a range's filter takes the SMs that the
+    // previous range's backprojection frees, ahead of that launch's
+    // remaining blocks
+    int least = 0, greatest = 0;
+    MONTE_CUDA(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    MONTE_CUDA(ctx, cudaStreamCreateWithPriority(&ctx->filter_stream, cudaStreamNonBlocking,
+                                                 greatest));
+  }
   for (cudaEvent_t& ev : ctx->pipe_ev)
     if (!ev) MONTE_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   ctx->pipe_ready = true;
@@ -434,6 +447,7 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, int stages,
   MONTE_CUDA(ctx, cudaEventRecord(ev[kEvStart], ctx->stream));
   MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_in, ev[kEvStart], 0));
   MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvStart], 0));
+  MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->filter_stream, ev[kEvStart], 0));
   for (int i = 0; i < nr; i++) {
     const size_t off = (size_t)r[i] * view_elems;
     MONTE_CUDA(ctx, cudaMemcpyAsync(din + off, src + off,
@@ -448,17 +462,23 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, int stages,
   for (int i = 0; i < nr; i++) {
     const size_t off = (size_t)r[i] * view_elems;
     const size_t bytes = (size_t)(r[i + 1] - r[i]) * view_elems * sizeof(float);
-    MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvIn + i], 0));
     if (do_filter) {
+      // filtered on its own stream as soon as it has landed, alongside the
+      // previous range's backprojection; the stream waits for it before
+      // the next backprojection (and before returning)
       monte_fdk_geom gr = *g;  // the range's views as a scan of their own
       gr.n_views = r[i + 1] - r[i];
-      MONTE_TRY(run_filter(ctx, &gr, dp + off, df + off, filter_mode));
+      MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->filter_stream, ev[kEvIn + i], 0));
+      MONTE_TRY(run_filter(ctx, &gr, dp + off, df + off, filter_mode, ctx->filter_stream));
+      MONTE_CUDA(ctx, cudaEventRecord(ev[kEvFilt + i], ctx->filter_stream));
+      MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvFilt + i], 0));
       if (filtered) {
-        MONTE_CUDA(ctx, cudaEventRecord(ev[kEvFilt + i], ctx->stream));
         MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ev[kEvFilt + i], 0));
         MONTE_CUDA(ctx, cudaMemcpyAsync(filtered + off, df + off, bytes, cudaMemcpyDeviceToHost,
                                         ctx->copy_out));
       }
+    } else {
+      MONTE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[kEvIn + i], 0));
     }
     if (!do_bp) continue;
     // the backprojection ranges trail the filtered ones by a view: with
@@ -517,6 +537,7 @@ int fdk_host_pipelined(monte_ctx* ctx, const monte_fdk_geom* g, int stages, cons
     // nothing may still read or write the caller's buffers after the return
     cudaStreamSynchronize(ctx->copy_in);
     cudaStreamSynchronize(ctx->copy_out);
+    if (ctx->filter_stream) cudaStreamSynchronize(ctx->filter_stream);
     cudaStreamSynchronize(ctx->stream);
   }
   return 1;

@@ -55,8 +55,9 @@ struct monte_ctx {
   int bp_tune_choice = -1;
   int last_bp_variant = -1;  // tile variant of the last backprojection, -1: plain kernel
   // host-memory FDK pipeline (created on first use): upload and download
-  // streams, and the events that order them against `stream`
-  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  // streams, a high-priority stream for the filter of each view range, and
+  // the events that order them against `stream`
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, filter_stream = nullptr;
   cudaEvent_t pipe_ev[24] = {};
   bool pipe_ready = false;
   int last_host_ranges = 0;  // view ranges of the last pipelined monte_fdk, 0: unpipelined
