@@ -186,6 +186,25 @@ def test_bad_arguments(ctx):
     assert int(prim.abs().sum()) == 0
 
 
+def test_empty_requests_change_nothing(ctx):
+    """Empty view or pixel ranges and zero histories per pixel are valid
+    requests that run no history and leave the tallies as they were."""
+    g = cfg1_geom(abi.MONTE_MC_STALE_SIN_PHI | abi.MONTE_MC_LOCAL_MAJORANT)
+    dev = cfg1_inputs("cuda")
+    prim = torch.full((g.n_views, g.nu, g.nv), 7, dtype=torch.int64, device="cuda")
+    scat = torch.full_like(prim, 3)
+    for req in (abi.mc_request(9, 4, (5, 5), (0, 64), (0, 64)),
+                abi.mc_request(9, 4, (0, 2), (10, 10), (0, 64)),
+                abi.mc_request(9, 4, (0, 2), (0, 64), (64, 64)),
+                abi.mc_request(9, 0, (0, 2), (0, 64), (0, 64))):
+        for kernel in (abi.MONTE_MC_PLAIN, abi.MONTE_MC_PERSISTENT):
+            req.kernel = kernel
+            st = ctx.mc_run(g, dev, req, prim, scat)
+            ctx.synchronize()
+            assert st["histories"] == 0, (kernel, st)
+    assert bool((prim == 7).all()) and bool((scat == 3).all())
+
+
 def test_fan_beam_one_row_detector_replay(ctx):
     """2-D (fan-beam) Monte Carlo with the same kernels.  The phantom is one
     z-invariant slice of the cylinder phantom (one voxel 100 cm tall) and
