@@ -551,7 +551,11 @@ int monte_siddon_forward(monte_ctx* ctx, const monte_mc_geom* g, const monte_sid
 /* Adjoint of monte_siddon_forward: grad_mu[v] += sum over rays of
  * (grad_line + grad_transmission * d exp(-L)/dL) * (length of the ray in
  * voxel v).  The line integrals are recomputed, not read back.  Either
- * gradient may be NULL.  Accumulation order is not fixed (float atomics). */
+ * gradient may be NULL.  The per-voxel sums are int64 fixed point, with a
+ * power-of-two scale chosen from the largest incoming gradient so that no
+ * sum can overflow, so grad_mu is the same bit for bit in every run
+ * whatever order the rays finish in; a non-finite incoming gradient makes
+ * grad_mu NaN. */
 int monte_siddon_backward(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid,
                           const float* mu, int view_begin, int view_end, const float* grad_line,
                           const float* grad_transmission, float* grad_mu, int mem);

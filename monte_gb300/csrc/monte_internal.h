@@ -81,6 +81,7 @@ enum ScratchSlot {
   kScratchStats = 11,
   kScratchFbp2 = 12,
   kScratchBpPad = 13,  // filtered projections with rows padded to 16 bytes (TMA)
+  kScratchSiddon = 14,  // the Siddon adjoint's fixed-point sums and scale
 };
 
 int set_error(monte_ctx* ctx, int code, const char* fmt, ...);

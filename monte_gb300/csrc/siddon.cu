@@ -10,8 +10,15 @@
 //    transmission;
 //  * siddon_backward_kernel: one thread per ray; recomputes the line
 //    integral (nothing from the forward pass is stored), then scatters
-//    dL/dmu_v = length in v, times the incoming gradient, into grad_mu with
-//    float atomics.
+//    dL/dmu_v = length in v, times the incoming gradient, into per-voxel
+//    int64 fixed-point sums.  Integer additions commute, so the gradient is
+//    the same bit for bit whatever order the rays' atomics land in (float
+//    atomics would round differently from run to run).  The scale is a
+//    power of two chosen on the device from the largest incoming gradient
+//    so that no sum can overflow: with |d exp(-L)/dL| <= 1, every ray adds
+//    at most (|grad_line| + |grad_transmission|) times the voxel diagonal
+//    to a voxel, and there are at most n_rays of them.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -72,21 +79,86 @@ __global__ void siddon_forward_kernel(SiddonDev s, const float* __restrict__ mu,
   if (trans) trans[cell] = expf(-L);
 }
 
+// The fixed-point scale of the adjoint's sums, in the scratch words after
+// them: [0] the largest |grad_line| + |grad_transmission| over the rays (as
+// float bits: non-negative floats order like their bit patterns), [1] the
+// scale as float bits, [2..3] 1 / scale as a double.
+struct SiddonScale {
+  unsigned gmax_bits;
+  unsigned scale_bits;
+  double inv_scale;
+};
+
+__global__ void siddon_gmax_kernel(SiddonDev s, const float* __restrict__ grad_line,
+                                   const float* __restrict__ grad_trans, SiddonScale* sc) {
+  const size_t nr = (size_t)(s.view_end - s.view_begin) * s.P.nu * s.P.nv;
+  float m = 0.f;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nr;
+       r += (size_t)gridDim.x * blockDim.x) {
+    const size_t cell = (size_t)s.view_begin * s.P.nu * s.P.nv + r;
+    const float g = (grad_line ? fabsf(grad_line[cell]) : 0.f) +
+                    (grad_trans ? fabsf(grad_trans[cell]) : 0.f);
+    m = g > m || g != g ? g : m;  // a NaN wins (its bits order above every finite value)
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = x > m || x != x ? x : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m != 0.f) atomicMax(&sc->gmax_bits, __float_as_uint(m));
+}
+
+// scale = 2^e with bound * scale <= 2^62, bound = gmax * diagonal * n_rays:
+// no voxel's sum can leave the int64 range.  A zero or non-finite gradient
+// leaves the scale at zero (the sums stay zero; a non-finite gradient then
+// makes grad_mu NaN in the conversion).
+__global__ void siddon_scale_kernel(SiddonScale* sc, double diag, double n_rays) {
+  const float g = __uint_as_float(sc->gmax_bits);
+  float scale = 0.f;
+  double inv = 0.0;
+  if (g > 0.f && isfinite(g)) {
+    int e;
+    frexp((double)g * diag * n_rays, &e);  // bound < 2^e
+    const int k = max(min(62 - e, 126), -126);  // bound * 2^k < 2^62
+    scale = ldexpf(1.f, k);
+    inv = ldexp(1.0, -k);
+  } else if (g != 0.f) {
+    inv = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+  }
+  sc->scale_bits = __float_as_uint(scale);
+  sc->inv_scale = inv;
+}
+
 __global__ void siddon_backward_kernel(SiddonDev s, const float* __restrict__ mu,
                                        const float* __restrict__ grad_line,
                                        const float* __restrict__ grad_trans,
-                                       float* __restrict__ grad_mu) {
+                                       unsigned long long* __restrict__ acc,
+                                       const SiddonScale* __restrict__ sc) {
   size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   int view, iu, iv;
   size_t cell;
   if (!ray_of(s, r, &view, &iu, &iv, &cell)) return;
+  const float scale = __uint_as_float(sc->scale_bits);
+  if (scale == 0.f) return;
   float o[3], d[3];
   siddon_ray(s.P, s.V, s.U, s.W, view, iu, iv, o, d);
   float gL = grad_line ? grad_line[cell] : 0.0f;
   if (grad_trans) gL -= grad_trans[cell] * expf(-line_integral(s, mu, o, d));  // dT/dL = -T
   if (gL == 0.0f) return;
-  siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2],
-              [&](size_t v, float len) { atomicAdd(grad_mu + v, gL * len); });
+  const float gs = gL * scale;  // exact: scale is a power of two
+  siddon_walk(s.g, o[0], o[1], o[2], d[0], d[1], d[2], [&](size_t v, float len) {
+    atomicAdd(acc + v, (unsigned long long)__float2ll_rn(gs * len));
+  });
+}
+
+// grad_mu += sums / scale
+__global__ void siddon_accumulate_kernel(const long long* __restrict__ acc,
+                                         const SiddonScale* __restrict__ sc, size_t n,
+                                         float* __restrict__ grad_mu) {
+  const double inv = sc->inv_scale;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    grad_mu[i] += (float)((double)acc[i] * inv);
 }
 
 int setup(monte_ctx* ctx, const monte_mc_geom* g, const monte_siddon_grid* grid, int vb, int ve,
@@ -210,6 +282,11 @@ int monte_siddon_backward(monte_ctx* ctx, const monte_mc_geom* g, const monte_si
   const size_t ncell = (size_t)g->n_views * g->nu * g->nv;
   const float *dmu = mu, *dgl = grad_line, *dgt = grad_transmission;
   float* dg = grad_mu;
+  // the fixed-point sums (int64 per voxel) and, after them, their scale
+  const size_t acc_bytes = nvox * sizeof(long long);
+  MONTE_TRY(ensure_slot(ctx, kScratchSiddon, acc_bytes + sizeof(SiddonScale), "gradient sums"));
+  unsigned long long* acc = (unsigned long long*)ctx->scratch[kScratchSiddon].ptr;
+  SiddonScale* sc = (SiddonScale*)((char*)ctx->scratch[kScratchSiddon].ptr + acc_bytes);
   if (mem == MONTE_MEM_HOST) {
     MONTE_TRY(ensure_slot(ctx, kScratchAux0, nvox * 4, "mu staging"));
     MONTE_TRY(ensure_slot(ctx, kScratchAux1, ncell * 4, "gradient staging"));
@@ -229,7 +306,16 @@ int monte_siddon_backward(monte_ctx* ctx, const monte_mc_geom* g, const monte_si
     MONTE_CUDA(ctx, cudaMemcpyAsync(dg, grad_mu, nvox * 4, cudaMemcpyHostToDevice, ctx->stream));
   }
   if (nr) {
-    siddon_backward_kernel<<<(unsigned)((nr + 127) / 128), 128, 0, ctx->stream>>>(s, dmu, dgl, dgt, dg);
+    MONTE_CUDA(ctx, cudaMemsetAsync(acc, 0, acc_bytes + sizeof(SiddonScale), ctx->stream));
+    const size_t cap = (size_t)std::max(ctx->sm_count, 1) * 8;  // grid-stride loops
+    const unsigned gblocks = (unsigned)std::min<size_t>((nr + 255) / 256, cap);
+    siddon_gmax_kernel<<<gblocks, 256, 0, ctx->stream>>>(s, dgl, dgt, sc);
+    const double diag = std::sqrt(grid->dx * grid->dx + grid->dy * grid->dy + grid->dz * grid->dz);
+    siddon_scale_kernel<<<1, 1, 0, ctx->stream>>>(sc, diag, (double)nr);
+    siddon_backward_kernel<<<(unsigned)((nr + 127) / 128), 128, 0, ctx->stream>>>(s, dmu, dgl, dgt,
+                                                                                  acc, sc);
+    const unsigned ablocks = (unsigned)std::min<size_t>((nvox + 255) / 256, cap);
+    siddon_accumulate_kernel<<<ablocks, 256, 0, ctx->stream>>>((const long long*)acc, sc, nvox, dg);
     MONTE_CUDA(ctx, cudaGetLastError());
   }
   if (mem == MONTE_MEM_HOST) {

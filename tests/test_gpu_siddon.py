@@ -2,7 +2,9 @@
 
 * line integrals match the FP64 Siddon oracle within 1e-5 relative;
 * the backward kernel is the adjoint of the forward (dot-product test) and
-  matches the FP64 gradient of exp(-L) and central finite differences;
+  matches the FP64 gradient of exp(-L) and central finite differences; its
+  fixed-point sums make it the same bit for bit in every run, and it adds
+  onto what grad_mu holds;
 * the Monte Carlo's primary tally agrees with exp(-L) (Beer-Lambert) per
   pixel within counting statistics.
 """
@@ -89,6 +91,38 @@ def test_backward_matches_central_differences(ctx):
         mm[v] -= h
         fd = (loss(mp) - loss(mm)) / (2 * h)
         assert abs(fd - grad[v]) < 1e-3 * abs(fd) + 1e-6, (v, fd, grad[v])
+
+
+def test_backward_is_bit_reproducible_and_accumulates(ctx):
+    g, grid, mu = _setup(3)
+    views = (0, 36)
+    rng = np.random.default_rng(11)
+    gl = torch.from_numpy(rng.standard_normal((g.n_views, g.nu, g.nv)).astype(np.float32)).cuda()
+    gt = torch.from_numpy(rng.random((g.n_views, g.nu, g.nv)).astype(np.float32)).cuda()
+    mu_d = torch.from_numpy(mu).cuda()
+    runs = []
+    for _ in range(3):
+        gm = torch.zeros_like(mu_d)
+        ctx.siddon_backward(g, grid, mu_d, views, gm, grad_line=gl, grad_transmission=gt)
+        ctx.synchronize()
+        runs.append(gm.cpu().numpy())
+    assert np.abs(runs[0]).max() > 0
+    assert all(np.array_equal(runs[0], r) for r in runs[1:])
+    # grad_mu accumulates: a second call adds the same gradient again
+    gm = torch.full_like(mu_d, 0.5)
+    ctx.siddon_backward(g, grid, mu_d, views, gm, grad_line=gl, grad_transmission=gt)
+    ctx.synchronize()
+    np.testing.assert_allclose(gm.cpu().numpy(), runs[0] + 0.5, rtol=1e-6, atol=1e-6)
+    # all-zero gradients add nothing; a NaN gradient poisons the result
+    gm = torch.full_like(mu_d, 2.0)
+    ctx.siddon_backward(g, grid, mu_d, views, gm, grad_line=torch.zeros_like(gl))
+    ctx.synchronize()
+    assert bool((gm == 2.0).all())
+    bad = gl.clone()
+    bad[1, 2, 3] = float("nan")
+    ctx.siddon_backward(g, grid, mu_d, views, gm, grad_line=bad)
+    ctx.synchronize()
+    assert bool(torch.isnan(gm).all())
 
 
 def test_mc_primary_tally_is_beer_lambert(ctx):
