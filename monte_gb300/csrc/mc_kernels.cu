@@ -240,12 +240,20 @@ __device__ __forceinline__ void persistent_body(const McDev& d) {
   warp_stats(d, st);
 }
 
-// 64 registers: four CTAs (32 warps) per SM.  Measured against 80 registers
-// (three CTAs) and a four-step flight with the label reads issued together,
-// this form has the highest throughput: the kernel is bound by issue, not by
-// the latency of the label gathers.
+// CTAs per SM: with local majorants (8-step rounds) 64 registers and four
+// CTAs (32 warps), with the single majorant (16-step rounds) 48 registers
+// and five.  Measured on 1e8 histories of the 325^3 phantom: local 4.00e9
+// histories/s at four CTAs against 3.89e9 at five and 3.80e9 at six (the
+// spills of the smaller budgets), single 1.95e9 at five against 1.90e9 at
+// four; 80 registers and three CTAs, and a four-step flight with the label
+// reads issued together, were slower still: the kernel is bound by issue,
+// not by the latency of the label gathers.
 template <int SR>
-__global__ void __launch_bounds__(256, 4) mc_persistent_kernel(McDev d) {
+struct McCtasPerSm {
+  static constexpr int value = SR == kStepsPerRoundLocal ? 4 : 5;
+};
+template <int SR>
+__global__ void __launch_bounds__(256, McCtasPerSm<SR>::value) mc_persistent_kernel(McDev d) {
   persistent_body<SR, kCollideBatch>(d);
 }
 
