@@ -262,8 +262,10 @@ __global__ void __launch_bounds__(256, McCtasPerSm<SR>::value) mc_persistent_ker
 // concatenated history ranges, and a lane that takes history h finds its
 // job by binary search over the range starts.  Everything else is the
 // single-job kernel's loop, reading the job's parameters through a pointer.
+// Four CTAs per SM (64 registers, some spilled): 1.609 s per 64-scan batch
+// against 1.635 s at three CTAs without spills.
 template <int SR>
-__global__ void __launch_bounds__(256, 3) mc_persistent_batch_kernel(
+__global__ void __launch_bounds__(256, 4) mc_persistent_batch_kernel(
     const McDev* __restrict__ jobs, const unsigned long long* __restrict__ starts, int n_jobs,
     unsigned long long total, unsigned long long* counter, unsigned long long* stats) {
   const unsigned FULL = 0xffffffffu;
