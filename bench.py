@@ -496,8 +496,9 @@ def diff_bench(ctx, device):
 
 
 def run_reference(args):
-    world, rank, local = dist_setup(args)
-    if rank != 0:
+    # rank 0 alone times the CPU implementation; no collective is needed,
+    # so no process group is created
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     g = geometry(args.small)
     vals = []
