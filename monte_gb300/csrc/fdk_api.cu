@@ -705,8 +705,14 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
   }
   const BpView* views = (const BpView*)ctx->fdk_views.ptr;
   const BpViewD* viewsd = (const BpViewD*)ctx->fdk_viewsd.ptr;
+  // every shape, the quick list's first (the leaders, in order of
+  // preference: a later shape has to be 1 % faster to displace one)
+  std::vector<int> order(kBpQuickCandidates, kBpQuickCandidates + kBpQuickCandidatesN);
+  for (int v = 0; v < fdk_bp_tiled_variants(); v++)
+    if (std::find(order.begin(), order.end(), v) == order.end()) order.push_back(v);
   int pick = -1;
-  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick, nullptr, 0, 3, padded));
+  MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick, order.data(), (int)order.size(), 3,
+                        padded));
   ctx->bp_tune_choice = pick;
   if (best) *best = pick;
   return monte_ctx_check_status(ctx);

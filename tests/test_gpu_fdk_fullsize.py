@@ -93,7 +93,7 @@ def test_full_size_tile_shapes_agree(ctx, scan):
     ref = None
     try:
         ref32 = None
-        for variant in (33, 29, 30, 24, 0, 22, 31, 37, 20, 34, 35, 36, 38, 39):
+        for variant in (33, 29, 30, 24, 0, 22, 31, 37, 20, 34, 35, 36, 38, 39, 40):
             ctx.set_bp_variant(variant)
             xy = torch.empty((g.nz, g.ny, g.nx), device="cuda")
             ctx.fdk_backproject(g, f, xy, mode=abi.MONTE_BP_TILED)
@@ -105,7 +105,7 @@ def test_full_size_tile_shapes_agree(ctx, scan):
                 if ref32 is None:
                     ref32 = xy
                 assert torch.equal(xy, ref32), variant
-            if variant in (20, 34, 35, 36, 38, 39):
+            if variant in (20, 34, 35, 36, 38, 39, 40):
                 err = rel_rms(xy.cpu().numpy(), ref.cpu().numpy())
                 assert err < 2e-6, (variant, err)
             else:
