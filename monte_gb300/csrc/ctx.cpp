@@ -136,6 +136,7 @@ int monte_ctx_destroy(monte_ctx* ctx) {
   monte::release(ctx->mc_mclass);
   monte::release(ctx->mc_label_copy);
   monte::release(ctx->mc_pixels);
+  monte::fdk_bp_footprints_release(&ctx->bp_footprints);
   if (ctx->d_status) cudaFree(ctx->d_status);
   for (cudaEvent_t ev : ctx->pipe_ev)
     if (ev) cudaEventDestroy(ev);

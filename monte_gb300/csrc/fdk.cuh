@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/monte.h"
+#include "bp_footprints.h"
 
 namespace monte {
 
@@ -100,7 +101,7 @@ int fdk_validate(monte_ctx* ctx, const monte_fdk_geom* g, bool need_grid);
 int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
                 const BpViewD* viewsd, const float* df, float* dv, int* best,
                 const int* candidates, int n_candidates, int reps,
-                const float* padded = nullptr);
+                const float* padded = nullptr, BpFootprints* footprints = nullptr);
 // Shapes that led on the reference-size workloads, for quick tuning.
 extern const int kBpQuickCandidates[];
 extern const int kBpQuickCandidatesN;
@@ -128,7 +129,12 @@ cudaError_t launch_fdk_bp_plain(const FdkDev& d, const BpView* views, const BpVi
 struct BpPart {
   int k_begin, k_end;
   const float* acc_in;
+  // set by launch_fdk_bp_tiled: the footprint table of the per-warp
+  // shapes (BpFootprints), or null (each warp projects its block's
+  // corners itself)
+  const int* footprints = nullptr;
 };
+
 // Counters after the status word (ints kBpExactSlot.. of the context's
 // status array, two uint64): voxel-view pairs the tiled backprojectors
 // decided in double (bp_ref_voxel) and (column, view) pairs whose distance
@@ -140,10 +146,12 @@ constexpr int kBpExactSlot = 8;
 // which the tiles are loaded when nu is not a multiple of 4 (a TMA row
 // stride must be a multiple of 16 bytes); the exact per-voxel path always
 // reads `filtered`.
+// footprints: the caller's table cache (see BpFootprints), or null.
 cudaError_t launch_fdk_bp_tiled(const FdkDev& d, const BpView* views, const BpViewD* viewsd,
                                 const float* filtered, float* vol_xy, float* vol_zy,
                                 int variant, int* status, cudaStream_t st,
-                                const BpPart* part = nullptr, const float* padded = nullptr);
+                                const BpPart* part = nullptr, const float* padded = nullptr,
+                                BpFootprints* footprints = nullptr);
 // Row pitch (floats) of the padded copy, and the copy itself, of views
 // [k_begin, k_end) (k_end < 0: to the last view).
 inline int fdk_bp_pad_pitch(int nu) { return (nu + 3) & ~3; }

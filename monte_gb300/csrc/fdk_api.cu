@@ -191,7 +191,8 @@ void build_fdk_tables(const monte_fdk_geom* g, FdkHostTables* t) {
 
 int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
                 const BpViewD* viewsd, const float* df, float* dv, int* best,
-                const int* candidates, int n_candidates, int reps, const float* padded) {
+                const int* candidates, int n_candidates, int reps, const float* padded,
+                BpFootprints* footprints) {
   FdkDev d = make_fdk_dev(*g);
   if (reps < 2) reps = 2;
   cudaEvent_t e0, e1;
@@ -207,7 +208,7 @@ int fdk_tune_bp(monte_ctx* ctx, const monte_fdk_geom* g, const BpView* views,
     for (int rep = 0; rep < reps; rep++) {
       cudaEventRecord(e0, ctx->stream);
       cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, dv, nullptr, v, ctx->d_status,
-                                          ctx->stream, nullptr, padded);
+                                          ctx->stream, nullptr, padded, footprints);
       cudaEventRecord(e1, ctx->stream);
       if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
         cudaEventDestroy(e0);
@@ -326,7 +327,7 @@ int run_bp(monte_ctx* ctx, const monte_fdk_geom* g, const float* d_filtered, flo
       ctx->last_bp_variant = -1;
     } else {
       e = launch_fdk_bp_tiled(d, views, viewsd, d_filtered, d_xy, d_zy, variant, ctx->d_status,
-                              ctx->stream, nullptr, padded);
+                              ctx->stream, nullptr, padded, &ctx->bp_footprints);
       ctx->last_bp_variant = variant;
     }
   } else {
@@ -494,7 +495,7 @@ int fdk_host_pipelined_body(monte_ctx* ctx, const monte_fdk_geom* g, int stages,
     }
     cudaError_t e = launch_fdk_bp_tiled(d, views, viewsd, df, last ? dvol_xy : dsum,
                                         last ? dvol_zy : nullptr, variant, ctx->d_status,
-                                        ctx->stream, &part, padded);
+                                        ctx->stream, &part, padded, &ctx->bp_footprints);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "backprojection launch");
     have_sum = true;
   }
@@ -712,7 +713,7 @@ int monte_fdk_autotune(monte_ctx* ctx, const monte_fdk_geom* g, int* best) {
     if (std::find(order.begin(), order.end(), v) == order.end()) order.push_back(v);
   int pick = -1;
   MONTE_TRY(fdk_tune_bp(ctx, g, views, viewsd, df, dv, &pick, order.data(), (int)order.size(), 3,
-                        padded));
+                        padded, &ctx->bp_footprints));
   ctx->bp_tune_choice = pick;
   if (best) *best = pick;
   return monte_ctx_check_status(ctx);

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/monte.h"
+#include "bp_footprints.h"
 
 namespace monte {
 
@@ -58,6 +59,8 @@ struct monte_ctx {
   // streams, a high-priority stream for the filter of each view range, and
   // the events that order them against `stream`
   cudaStream_t copy_in = nullptr, copy_out = nullptr, filter_stream = nullptr;
+  // footprint table of the tiled backprojector's last geometry and shape
+  monte::BpFootprints bp_footprints;
   cudaEvent_t pipe_ev[24] = {};
   bool pipe_ready = false;
   int last_host_ranges = 0;  // view ranges of the last pipelined monte_fdk, 0: unpipelined
