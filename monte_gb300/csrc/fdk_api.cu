@@ -17,7 +17,7 @@
 namespace monte {
 
 FdkDev make_fdk_dev(const monte_fdk_geom& g) {
-  FdkDev d;
+  FdkDev d{};  // every byte defined: the tile caches compare FdkDev bytes
   d.x0d = g.x0;
   d.y0d = g.y0;
   d.z0d = g.z0;
