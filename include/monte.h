@@ -19,6 +19,10 @@
  *     through device buffers it owns and copies results back before returning.
  *   - One context per host thread; a context owns one CUDA stream.  Device
  *     calls are asynchronous on that stream unless `mem` is MONTE_MEM_HOST.
+ *   - A context keeps grow-only device buffers until it is destroyed:
+ *     staging and scratch arrays, per-geometry tables, and the tiled
+ *     backprojector's footprint table of its last geometry (4 bytes per
+ *     block of voxel columns and view, at most 256 MB).
  *   - There is no CPU fallback: without a usable GPU every compute call fails
  *     with MONTE_ECUDA.
  *
