@@ -64,9 +64,12 @@ int monte_ctx_destroy(monte_ctx* ctx);
  * monte_ctx_create when ctx is NULL). Never NULL. */
 const char* monte_last_error(const monte_ctx* ctx);
 /* Queue the context's work on a caller-provided cudaStream_t; NULL means
- * the CUDA legacy default stream (stream 0). */
+ * the CUDA legacy default stream (stream 0).  A switch first waits for the
+ * work the context queued on its current stream (its buffers are reused by
+ * the next call), so that stream must still exist; the new one must stay
+ * valid while the context uses it. */
 int monte_ctx_set_stream(monte_ctx* ctx, void* cuda_stream);
-/* Go back to the context's own non-blocking stream. */
+/* Go back to the context's own non-blocking stream (waiting as above). */
 int monte_ctx_use_own_stream(monte_ctx* ctx);
 /* Wait for all work queued on the context's stream. */
 int monte_ctx_synchronize(monte_ctx* ctx);

@@ -156,16 +156,25 @@ const char* monte_last_error(const monte_ctx* ctx) {
   return copy.c_str();
 }
 
+// The context's scratch buffers and tables are reused by the next call,
+// which nothing would order after work still queued on the old stream: a
+// switch waits for that work first.
+static int switch_stream(monte_ctx* ctx, cudaStream_t next) {
+  if (next == ctx->stream) return MONTE_OK;
+  MONTE_TRY(monte::enter(ctx));
+  MONTE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->stream = next;
+  return MONTE_OK;
+}
+
 int monte_ctx_set_stream(monte_ctx* ctx, void* cuda_stream) {
   if (!ctx) return MONTE_EINVAL;
-  ctx->stream = (cudaStream_t)cuda_stream;
-  return MONTE_OK;
+  return switch_stream(ctx, (cudaStream_t)cuda_stream);
 }
 
 int monte_ctx_use_own_stream(monte_ctx* ctx) {
   if (!ctx) return MONTE_EINVAL;
-  ctx->stream = ctx->own_stream;
-  return MONTE_OK;
+  return switch_stream(ctx, ctx->own_stream);
 }
 
 int monte_ctx_synchronize(monte_ctx* ctx) {
